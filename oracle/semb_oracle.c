@@ -1,0 +1,45 @@
+/* Oracle for the CMP/CRS semblance search: a CPU restatement of the reference's
+ * OpenMP programs (CMP/OpenMP/src/main.cpp, CRS/OpenMP/src/main.cpp).
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/ as the checker of the CUDA path and by
+ * bench.py as the timed CPU baseline.  It is never linked into the product.
+ *
+ * Parity pinning: tests/test_oracle_pins.py runs the reference's own programs
+ * (built from their sources by this directory's Makefile into _ref/) on seeded
+ * synthetic inputs and requires this restatement to reproduce their SU outputs
+ * bit for bit; tests/golden/ holds those reference outputs so the pin also holds
+ * where the reference tree is absent.
+ *
+ * Constants follow the reference: EPSILON 1e-13 and FACTOR 1e6 (both files'
+ * :41-43), MAX_W 16 for CMP (CMP/OpenMP/src/main.cpp:39) and 5 for CRS
+ * (CRS/OpenMP/src/main.cpp:39; the reference never checks it, here a larger
+ * window is an error). */
+#include <math.h>
+#include <omp.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define EPSILON 1e-13
+#define FACTOR 1e6
+#define MAX_W_CMP 16
+#define MAX_W_CRS 5
+
+#define REAL float
+#define SQRTR sqrtf
+#define SFX _f32
+#include "semb_oracle_body.h"
+#undef REAL
+#undef SQRTR
+#undef SFX
+
+#define REAL double
+#define SQRTR sqrt
+#define SFX _f64
+#include "semb_oracle_body.h"
+#undef REAL
+#undef SQRTR
+#undef SFX
+
+int semb_oracle_max_threads(void) { return omp_get_max_threads(); }
+void semb_oracle_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }

@@ -1,0 +1,328 @@
+/* Body of the oracle restatement, instantiated once per precision by semb_oracle.c
+ * with REAL (float|double), SQRTR (sqrtf|sqrt) and SFX (function-name suffix).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a CPU restatement of the reference's OpenMP
+ * semblance search (CMP/OpenMP/src/main.cpp:67-260, CRS/OpenMP/src/main.cpp:84-359)
+ * written as plain C.  Every arithmetic expression keeps the reference's operand
+ * order and types (float/double promotion of the literals included) so that, built
+ * with -ffp-contract=off, it reproduces the reference bit for bit.  It is the
+ * checker for the CUDA path and the CPU baseline of the benchmark; nothing in the
+ * product links it.
+ *
+ * Inputs are the arrays su_gather::linearize produces (CRS/OpenMP/src/su_gather.cpp:
+ * 94-127): an inclusive prefix count of traces per CDP, the samples of all traces
+ * back to back, and the raw integer header fields gx, gy, sx, sy, scalco per trace.
+ * Parameters are passed as the values the reference's parser produced: stof()
+ * results for CMP, stod() results for CRS, both widened to double.
+ *
+ * Divergence (documented): where the reference converts a NaN or out-of-int-range
+ * traveltime with (int)t, which is undefined behaviour in C (x86 gives INT_MIN and
+ * the window test then depends on signed overflow; AArch64 saturates), this
+ * restatement counts the trace as out of range.  Such traveltimes need a negative
+ * t0^2 + c*h (a negative -c0) or a window past 2^31 samples. */
+
+#define CAT_(a, b) a##b
+#define CAT(a, b) CAT_(a, b)
+
+/* (int)t with the reference's meaning for every t the reference handles; returns 0
+ * and sets *bad when t is NaN or outside the int range. */
+static inline int CAT(trunc_int, SFX)(REAL t, int* bad) {
+  if (!(t > -2147483648.0 && t < 2147483647.0)) { *bad = 1; return 0; }
+  return (int)t;
+}
+
+/* CMP: CMP/OpenMP/src/main.cpp:88-241 (grid :119-122, half-offsets :125-136,
+ * semblance :149-204, argmax :207-222, output values :253-255). */
+int CAT(semb_oracle_cmp, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int ns, int dt_us,
+                              const float* samples, const int32_t* gxi, const int32_t* gyi,
+                              const int32_t* sxi, const int32_t* syi, const int32_t* scalcoi,
+                              double c0_parsed, double c1_parsed, int nc, double tau_parsed,
+                              int32_t* ctr, REAL* str, REAL* stk, float* out_c,
+                              REAL* sem_all, double* seconds) {
+  const REAL c0 = (REAL)(c0_parsed * FACTOR);
+  const REAL c1 = (REAL)(c1_parsed * FACTOR);
+  const REAL itau = (REAL)tau_parsed;
+  if (ncdps <= 0 || nc <= 0 || ns <= 0) return -1;
+  const int ttraces = ntraces_by_cdp_id[ncdps - 1];
+  const REAL inc = (c1 - c0) * (1.0f / (REAL)nc);
+
+  REAL* c = (REAL*)malloc(sizeof(REAL) * (size_t)nc);
+  REAL* h = (REAL*)malloc(sizeof(REAL) * (size_t)(ttraces > 0 ? ttraces : 1));
+  REAL* num = (REAL*)malloc(sizeof(REAL) * (size_t)ns * nc);
+  REAL* stt = (REAL*)malloc(sizeof(REAL) * (size_t)ns * nc);
+  if (!c || !h || !num || !stt) { free(c); free(h); free(num); free(stt); return -2; }
+
+  REAL dt = (REAL)dt_us;
+  dt = dt / 1000000.0f;
+  REAL idt = 1.0f / dt;
+  int tau = ((int)(itau * idt) > 0) ? ((int)(itau * idt)) : 0;
+  REAL w = (2 * tau) + 1;
+  if (w > MAX_W_CMP) { free(c); free(h); free(num); free(stt); return -3; }
+
+  double t_beg = omp_get_wtime();
+  for (int i = 0; i < nc; i++) c[i] = c0 + inc * i;
+
+#pragma omp parallel for
+  for (int i = 0; i < ttraces; i++) {
+    REAL _s = (REAL)scalcoi[i];
+    if (-EPSILON < _s && _s < EPSILON) _s = 1.0;
+    else if (_s < 0) _s = 1.0f / _s;
+    REAL hx = ((REAL)gxi[i] - (REAL)sxi[i]) * _s;
+    REAL hy = ((REAL)gyi[i] - (REAL)syi[i]) * _s;
+    h[i] = 0.25 * (hx * hx + hy * hy) / FACTOR;
+  }
+
+  for (int cdp_id = 0; cdp_id < ncdps; cdp_id++) {
+    const int t_id0 = cdp_id > 0 ? ntraces_by_cdp_id[cdp_id - 1] : 0;
+    const int t_idf = ntraces_by_cdp_id[cdp_id];
+    const float* cdpsmpl = samples + (size_t)t_id0 * ns;
+
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < ns * nc; i++) {
+      REAL _num[MAX_W_CMP], _ac_squared = 0, _ac_linear = 0, _den = 0, m = 0;
+      int err = 0;
+      int c_id = i % nc;
+      int t0 = i / nc;
+      REAL _c = c[c_id];
+      REAL _t0 = dt * t0;
+      _t0 = _t0 * _t0;
+      for (int j = 0; j < w; j++) _num[j] = 0.0f;
+      for (int t_id = t_id0; t_id < t_idf; t_id++) {
+        REAL t = SQRTR(_t0 + _c * h[t_id]) * idt;
+        int bad = 0;
+        int it = CAT(trunc_int, SFX)(t, &bad);
+        int ittau = it - tau;
+        REAL x = t - (REAL)it;
+        if (!bad && ittau >= 0 && it + tau + 1 < ns) {
+          size_t k1 = (size_t)ittau + (size_t)(t_id - t_id0) * ns;
+          REAL sk1p1 = cdpsmpl[k1], sk1;
+          for (int j = 0; j < w; j++) {
+            k1++;
+            sk1 = sk1p1;
+            sk1p1 = cdpsmpl[k1];
+            REAL v = (sk1p1 - sk1) * x + sk1;
+            _num[j] += v;
+            _den += v * v;
+            _ac_linear += v;
+          }
+          m++;
+        } else {
+          err++;
+        }
+      }
+      for (int j = 0; j < w; j++) _ac_squared += _num[j] * _num[j];
+      if (_den > EPSILON && m > EPSILON && w > EPSILON && err < 2) {
+        num[i] = _ac_squared / (_den * m);
+        stt[i] = _ac_linear / (w * m);
+      } else {
+        num[i] = -1.0f;
+        stt[i] = -1.0f;
+      }
+    }
+
+    if (sem_all) memcpy(sem_all + (size_t)cdp_id * ns * nc, num, sizeof(REAL) * (size_t)ns * nc);
+
+#pragma omp parallel for
+    for (int t0 = 0; t0 < ns; t0++) {
+      REAL max_sem = 0.0f;
+      int max_c = -1;
+      for (int it = t0 * nc; it < (t0 + 1) * nc; it++) {
+        if (num[it] > max_sem) { max_sem = num[it]; max_c = it; }
+      }
+      size_t o = (size_t)cdp_id * ns + t0;
+      ctr[o] = max_c % nc;
+      str[o] = max_sem;
+      stk[o] = max_c > -1 ? stt[max_c] : 0.0f;
+    }
+  }
+  if (seconds) *seconds = omp_get_wtime() - t_beg;
+
+  if (out_c) {
+    for (size_t o = 0; o < (size_t)ncdps * ns; o++)
+      out_c[o] = ctr[o] < 0 ? 0.0f : (c0 + inc * ctr[o]) / FACTOR;
+  }
+  free(c); free(h); free(num); free(stt);
+  return 0;
+}
+
+/* CRS: CRS/OpenMP/src/main.cpp:85-359 (grid :155-160, geometry :163-177, aperture
+ * :179-204 and :289-317, semblance :209-267, argmax :270-285, outputs :348-352).
+ * nbr_off[ncdps+1] / nbr[] hold each CDP's neighbour list in ascending order
+ * (su_gather.cpp:70-87). */
+int CAT(semb_oracle_crs, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int ns, int dt_us,
+                              const float* samples, const int32_t* gxi, const int32_t* gyi,
+                              const int32_t* sxi, const int32_t* syi, const int32_t* scalcoi,
+                              const int32_t* nbr_off, const int32_t* nbr,
+                              double a0_parsed, double a1_parsed, int na,
+                              double b0_parsed, double b1_parsed, int nb,
+                              double c0_parsed, double c1_parsed, int nc, double tau_parsed,
+                              int32_t* ctr, REAL* str, REAL* stk,
+                              float* out_a, float* out_b, float* out_c,
+                              REAL* sem_all, double* seconds, int64_t* n_semblance_traces) {
+  const REAL a0 = (REAL)a0_parsed, a1 = (REAL)a1_parsed;
+  const REAL b0 = (REAL)b0_parsed, b1 = (REAL)b1_parsed;
+  const REAL c0 = (REAL)(c0_parsed * FACTOR), c1 = (REAL)(c1_parsed * FACTOR);
+  const REAL itau = (REAL)tau_parsed;
+  if (ncdps <= 0 || na <= 0 || nb <= 0 || nc <= 0 || ns <= 0) return -1;
+  const int ttraces = ntraces_by_cdp_id[ncdps - 1];
+  const REAL inc_a = (a1 - a0) * (1.0 / (REAL)na);
+  const REAL inc_b = (b1 - b0) * (1.0 / (REAL)nb);
+  const REAL inc_c = (c1 - c0) * (1.0 / (REAL)nc);
+  const int npar = na * nb * nc;
+
+  int max_ap = 0;
+  for (int i = 0; i < ncdps; i++) {
+    int n = 0;
+    for (int q = nbr_off[i]; q < nbr_off[i + 1]; q++) {
+      int cdp = nbr[q];
+      n += ntraces_by_cdp_id[cdp] - (cdp > 0 ? ntraces_by_cdp_id[cdp - 1] : 0);
+    }
+    if (n > max_ap) max_ap = n;
+  }
+
+  REAL* pa = (REAL*)malloc(sizeof(REAL) * (size_t)npar);
+  REAL* pb = (REAL*)malloc(sizeof(REAL) * (size_t)npar);
+  REAL* pc = (REAL*)malloc(sizeof(REAL) * (size_t)npar);
+  REAL* h0 = (REAL*)malloc(sizeof(REAL) * (size_t)(ttraces > 0 ? ttraces : 1));
+  REAL* m0x = (REAL*)malloc(sizeof(REAL) * (size_t)(ttraces > 0 ? ttraces : 1));
+  REAL* m0y = (REAL*)malloc(sizeof(REAL) * (size_t)(ttraces > 0 ? ttraces : 1));
+  REAL* num = (REAL*)malloc(sizeof(REAL) * (size_t)ns * npar);
+  REAL* stt = (REAL*)malloc(sizeof(REAL) * (size_t)ns * npar);
+  size_t apn = (size_t)(max_ap > 0 ? max_ap : 1);
+  float* cdpsmpl = (float*)malloc(sizeof(float) * apn * ns);
+  REAL* m2 = (REAL*)malloc(sizeof(REAL) * apn);
+  REAL* m = (REAL*)malloc(sizeof(REAL) * apn);
+  REAL* h = (REAL*)malloc(sizeof(REAL) * apn);
+  if (!pa || !pb || !pc || !h0 || !m0x || !m0y || !num || !stt || !cdpsmpl || !m2 || !m || !h) {
+    free(pa); free(pb); free(pc); free(h0); free(m0x); free(m0y); free(num); free(stt);
+    free(cdpsmpl); free(m2); free(m); free(h);
+    return -2;
+  }
+
+  REAL dt = (REAL)dt_us;
+  dt = dt / 1000000.0f;
+  REAL idt = 1.0f / dt;
+  int tau = (int)(itau * idt) > 0 ? (int)(itau * idt) : 0;
+  int w = (2 * tau) + 1;
+  int rc = 0;
+  if (w > MAX_W_CRS) rc = -3;
+  int64_t nsem = 0;
+
+  double t_beg = omp_get_wtime();
+  for (int i = 0; rc == 0 && i < npar; i++) {
+    pa[i] = a0 + inc_a * (i / (nc * nb));
+    pb[i] = b0 + inc_b * ((i / nc) % nb);
+    pc[i] = c0 + inc_c * (i % nc);
+  }
+
+#pragma omp parallel for
+  for (int i = 0; i < ttraces; i++) {
+    REAL _s = (REAL)scalcoi[i];
+    if (-EPSILON < _s && _s < EPSILON) _s = 1.0;
+    else if (_s < 0) _s = 1.0f / _s;
+    m0x[i] = ((REAL)gxi[i] + (REAL)sxi[i]) * _s * 0.5;
+    m0y[i] = ((REAL)gyi[i] + (REAL)syi[i]) * _s * 0.5;
+    REAL hx = ((REAL)gxi[i] - (REAL)sxi[i]) * _s;
+    REAL hy = ((REAL)gyi[i] - (REAL)syi[i]) * _s;
+    h0[i] = 0.25 * (hx * hx + hy * hy) / FACTOR;
+  }
+
+  for (int cdp_id = 0; rc == 0 && cdp_id < ncdps; cdp_id++) {
+    const int first = cdp_id > 0 ? ntraces_by_cdp_id[cdp_id - 1] : 0;
+    const REAL m0x_cdp_id = m0x[first], m0y_cdp_id = m0y[first];
+    int size = 0;
+    for (int q = nbr_off[cdp_id]; q < nbr_off[cdp_id + 1]; q++) {
+      int cdp = nbr[q];
+      int t_id0 = cdp > 0 ? ntraces_by_cdp_id[cdp - 1] : 0;
+      int t_idf = ntraces_by_cdp_id[cdp];
+      memcpy(cdpsmpl + (size_t)size * ns, samples + (size_t)t_id0 * ns, sizeof(float) * (size_t)(t_idf - t_id0) * ns);
+      for (int it = 0; it < t_idf - t_id0; it++) {
+        REAL dx = m0x[t_id0 + it] - m0x_cdp_id;
+        REAL dy = m0y[t_id0 + it] - m0y_cdp_id;
+        REAL _m2 = dx * dx + dy * dy;
+        m2[size + it] = _m2;
+        m[size + it] = SQRTR(_m2);
+        h[size + it] = h0[t_id0 + it];
+      }
+      size += t_idf - t_id0;
+    }
+    nsem += size;
+
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int t0 = 0; t0 < ns; t0++) {
+      for (int par_id = 0; par_id < npar; par_id++) {
+        REAL _num[MAX_W_CRS], _ac_squared = 0, _ac_linear = 0, _den = 0, mm = 0;
+        int err = 0;
+        int id = t0 * npar + par_id;
+        REAL pA = pa[par_id], pB = pb[par_id], pC = pc[par_id];
+        REAL _t0 = dt * t0;
+        for (int j = 0; j < w; j++) _num[j] = 0.0f;
+        for (int k = 0; k < size; k++) {
+          REAL _m2 = m2[k];
+          REAL t = _t0 + pA * m[k];
+          t = t * t + pB * _m2 + pC * h[k];
+          t = t < 0.0 ? -1 : SQRTR(t);
+          int bad = 0;
+          int it = CAT(trunc_int, SFX)(t * idt, &bad);
+          int ittau = it - tau;
+          REAL x = t * idt - (REAL)it;
+          if (!bad && ittau >= 0 && it + tau + 1 < ns) {
+            size_t k1 = (size_t)ittau + (size_t)k * ns;
+            REAL sk1p1 = cdpsmpl[k1], sk1;
+            for (int j = 0; j < w; j++) {
+              k1++;
+              sk1 = sk1p1;
+              sk1p1 = cdpsmpl[k1];
+              REAL v = (sk1p1 - sk1) * x + sk1;
+              _num[j] += v;
+              _den += v * v;
+              _ac_linear += v;
+            }
+            mm++;
+          } else {
+            err++;
+          }
+        }
+        for (int j = 0; j < w; j++) _ac_squared += _num[j] * _num[j];
+        if (_den > EPSILON && mm > EPSILON && w > EPSILON && err < 2) {
+          num[id] = _ac_squared / (_den * mm);
+          stt[id] = _ac_linear / (w * mm);
+        } else {
+          num[id] = 0.0f;
+          stt[id] = 0.0f;
+        }
+      }
+    }
+
+    if (sem_all) memcpy(sem_all + (size_t)cdp_id * ns * npar, num, sizeof(REAL) * (size_t)ns * npar);
+
+#pragma omp parallel for
+    for (int t0 = 0; t0 < ns; t0++) {
+      REAL max_sem = 0.0f;
+      int max_par = 0;
+      for (int it = t0 * npar; it < (t0 + 1) * npar; it++) {
+        if (num[it] > max_sem) { max_sem = num[it]; max_par = it; }
+      }
+      size_t o = (size_t)cdp_id * ns + t0;
+      ctr[o] = max_par % npar;
+      str[o] = max_sem;
+      stk[o] = stt[max_par];
+    }
+  }
+  if (seconds) *seconds = omp_get_wtime() - t_beg;
+  if (n_semblance_traces) *n_semblance_traces = nsem;
+
+  if (rc == 0) {
+    for (size_t o = 0; o < (size_t)ncdps * ns; o++) {
+      if (out_a) out_a[o] = (a0 + inc_a * (ctr[o] / (nc * nb)));
+      if (out_b) out_b[o] = (b0 + inc_b * ((ctr[o] / nc) % nb));
+      if (out_c) out_c[o] = (c0 + inc_c * (ctr[o] % nc)) / FACTOR;
+    }
+  }
+  free(pa); free(pb); free(pc); free(h0); free(m0x); free(m0y); free(num); free(stt);
+  free(cdpsmpl); free(m2); free(m); free(h);
+  return rc;
+}
+
+#undef CAT
+#undef CAT_
