@@ -1,0 +1,221 @@
+/* semb_gb300.h - C ABI of the GB300 CMP/CRS semblance search and stack.
+ *
+ * The reference (cuplgb/IPDPS-CRS-CMP-code) has no library: each of its programs
+ * is one main() that reads an SU file, searches, and writes SU files.  This ABI
+ * exposes the same path as four steps a foreign-function caller can bind with
+ * plain pointers and sizes:
+ *
+ *   ingest   semb_survey_load / semb_survey_view      <- su_gather + linearize
+ *   setup    semb_plan_create / semb_plan_upload      <- parameter grid, per-trace
+ *                                                        geometry, neighbour lists
+ *   search   semb_plan_run                            <- per-CDP semblance loop,
+ *                                                        argmax and stack
+ *   output   semb_plan_download / semb_survey_write   <- result arrays, SU writer
+ *
+ * Conventions: every function returns an int status (SEMB_OK = 0) instead of
+ * exiting the process as the reference's LOG(FAIL) does (CMP/OpenMP/src/log.cpp:
+ * 44-46); semb_last_error() gives a message for the calling thread.  Host buffers
+ * belong to the caller.  A plan owns its device memory and one CUDA stream; plans
+ * are not shared between threads.  Nothing here falls back to the CPU: without a
+ * usable GPU, semb_plan_create fails with SEMB_E_NODEV.
+ */
+#ifndef SEMB_GB300_H
+#define SEMB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEMB_ABI_VERSION 1
+
+/* Methods. */
+enum { SEMB_CMP = 0, SEMB_CRS = 1 };
+
+/* Search forms.
+ *  SEMB_PLAIN_F32 : FP32 throughout, the reference's arithmetic order (no fused
+ *                   multiply-add, IEEE sqrt/div); results match the reference's
+ *                   single-precision OpenMP build.
+ *  SEMB_BATCHED   : persistent kernel over an aperture-sorted work queue, traces
+ *                   stored as FP16/BF16 with a per-trace FP32 scale (or FP32),
+ *                   FP32 interpolation and sums with compensated energy sums,
+ *                   top-4 candidates kept per (CDP, t0) and re-evaluated in FP64
+ *                   where the best two are closer than `repick_gap`. */
+enum { SEMB_PLAIN_F32 = 0, SEMB_BATCHED = 1 };
+enum { SEMB_STORE_F32 = 0, SEMB_STORE_F16 = 1, SEMB_STORE_BF16 = 2 };
+enum { SEMB_REPICK_OFF = 0, SEMB_REPICK_NEAR_TIES = 1, SEMB_REPICK_ALWAYS = 2 };
+
+/* Status codes. */
+enum {
+  SEMB_OK = 0,
+  SEMB_E_ARG = 1,       /* invalid argument or parameter */
+  SEMB_E_IO = 2,        /* file could not be opened, read or written */
+  SEMB_E_FORMAT = 3,    /* malformed SU data (truncated trace, mixed ns, ...) */
+  SEMB_E_WINDOW = 4,    /* semblance window 2*tau/dt+1 above the method's maximum */
+  SEMB_E_NOMEM = 5,     /* host or device allocation failed */
+  SEMB_E_CUDA = 6,      /* a CUDA call failed */
+  SEMB_E_TIMEOUT = 7,   /* a bounded device-side wait gave up */
+  SEMB_E_STATE = 8,     /* call out of order (e.g. run before upload) */
+  SEMB_E_NODEV = 9      /* no usable CUDA device */
+};
+
+/* Search parameters, with the meaning of the reference's command-line flags
+ * (CMP/OpenMP/src/main.cpp:57-74, CRS/OpenMP/src/main.cpp:67-98).  Numbers are the
+ * values the reference's parser produces: for CMP the flags are read with stof,
+ * so pass values already rounded to float; for CRS with stod.  c0/c1 are in s^2/m^2
+ * (the library applies the reference's 1e6 scale); tau in seconds. */
+typedef struct semb_params {
+  int32_t method;        /* SEMB_CMP | SEMB_CRS */
+  int32_t mode;          /* SEMB_PLAIN_F32 | SEMB_BATCHED */
+  double a0, a1;         /* CRS only: -a0 -a1 */
+  double b0, b1;         /* CRS only: -b0 -b1 */
+  double c0, c1;         /* -c0 -c1 */
+  int32_t na, nb, nc;    /* -na -nb (CRS only) -nc */
+  int32_t aph;           /* -aph: half-offset aperture (m), applied at ingest */
+  int32_t apm;           /* -apm: midpoint aperture (m), CRS only */
+  int32_t storage;       /* SEMB_STORE_*, batched form only */
+  double tau;            /* -tau: half window (s) */
+  double azimuth;        /* -azimuth (deg): accepted; the reference's CRS operator
+                            uses the unsigned midpoint distance, which this
+                            search keeps, so it does not change results */
+  int32_t repick;        /* SEMB_REPICK_*, batched form only */
+  float repick_gap;      /* near-tie threshold on semblance (batched form) */
+} semb_params;
+
+/* Fill `p` with the defaults for `method` (grid fields zero, batched FP16 with
+ * near-tie re-pick at gap 2e-3).  Replaces nothing in the reference. */
+void semb_params_init(semb_params* p, int32_t method);
+
+/* A linearized gather: what su_gather::linearize hands to the search
+ * (CRS/OpenMP/src/su_gather.cpp:94-127), with 64-bit counts.  Traces of one CDP
+ * are contiguous; cdp_end[i] is the inclusive prefix count of traces up to CDP i
+ * (the reference's ntraces_by_cdp_id).  Header integers are the raw SU fields. */
+typedef struct semb_gather_view {
+  int32_t ncdps;
+  int32_t ns;            /* samples per trace */
+  int32_t dt_us;         /* SU dt of the first trace of the first CDP (microseconds) */
+  int32_t reserved;
+  int64_t ntraces;
+  const int64_t* cdp_end;    /* [ncdps] */
+  const int32_t* cdp;        /* [ncdps] cdp header value of each CDP (may be NULL) */
+  const int32_t* gx;         /* [ntraces] */
+  const int32_t* gy;
+  const int32_t* sx;
+  const int32_t* sy;
+  const int32_t* scalco;
+  const float* samples;      /* [ntraces * ns], trace-major */
+} semb_gather_view;
+
+/* ---- ingest (host) ---------------------------------------------------------- */
+
+typedef struct semb_survey semb_survey;
+
+/* Read an SU file and group it as the reference does: traces whose half-offset
+ * exceeds aph are dropped, traces are grouped by their cdp header in ascending
+ * order, keeping file order inside a CDP (CRS/OpenMP/src/su_gather.cpp:33-65);
+ * for SEMB_CMP the CDPs are then ordered by decreasing fold with the reference's
+ * std::sort (CMP/OpenMP/src/su_gather.cpp:68).  Replaces su_gather::su_gather. */
+int semb_survey_load(const char* path, int32_t method, int32_t aph, semb_survey** out);
+
+/* Same, from SU bytes already in memory (headers and samples interleaved exactly
+ * as in a file). */
+int semb_survey_from_bytes(const void* su_bytes, int64_t nbytes, int32_t method, int32_t aph,
+                           semb_survey** out);
+
+/* Borrow the survey's linearized arrays (valid until semb_survey_free).
+ * Replaces su_gather::linearize (CRS/OpenMP/src/su_gather.cpp:94-127). */
+int semb_survey_view(const semb_survey* s, semb_gather_view* out);
+
+/* Write the reference's output files into out_dir: cmp.{c,coher,stack}.su or
+ * crs.{a,b,c,coher,stack}.su, one trace per CDP in the survey's CDP order, each a
+ * copy of the CDP's first trace header with offset 0 and sx=gx, sy=gy set to the
+ * integer midpoint (CRS/OpenMP/src/main.cpp:331-359).  ctr/str/stk are
+ * [ncdps * ns] as returned by semb_plan_download. */
+int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t* ctr,
+                      const float* str, const float* stk, const char* out_dir);
+
+void semb_survey_free(semb_survey* s);
+
+/* ---- search (device) -------------------------------------------------------- */
+
+typedef struct semb_plan semb_plan;
+
+/* Validate parameters and create a plan on CUDA device `device` (its own stream).
+ * Replaces the set-up in main (CMP/OpenMP/src/main.cpp:67-110,
+ * CRS/OpenMP/src/main.cpp:84-138) and the reference CUDA device wrapper
+ * (CMP/CUDA/src/cuda.cpp:139-175). */
+int semb_plan_create(const semb_params* p, int32_t device, semb_plan** out);
+
+/* Copy a gather to the device and build everything the search reads: the FP32
+ * (and, batched, FP16/BF16 + scale) trace store, per-trace half-offsets and
+ * midpoints, the per-CDP neighbour lists within apm (CRS), the per-CDP aperture
+ * index lists with |dm|, dm^2, h per entry, the candidate grid and the work queue.
+ * Replaces CMP/OpenMP/src/main.cpp:118-143 and CRS/OpenMP/src/main.cpp:154-204,
+ * 289-317 (and the reference CUDA kernels init_c, init_half, init_par, init_mid,
+ * compute_points_for_gather: CMP/CUDA/src/main.cu:61-83, CRS/CUDA/src/main.cu:61-150).
+ * Synchronous: on return the caller's buffers may be reused. */
+int semb_plan_upload(semb_plan* plan, const semb_gather_view* g);
+
+/* Search every CDP of the uploaded gather and keep, per (CDP, t0), the picked
+ * candidate index, its semblance and its stack on the device.  Replaces the
+ * per-CDP loop (CMP/OpenMP/src/main.cpp:146-236, CRS/OpenMP/src/main.cpp:207-320)
+ * and the CUDA kernels compute_semblances + redux_semblances
+ * (CMP/CUDA/src/main.cu:87-173, CRS/CUDA/src/main.cu:154-264).  Synchronous. */
+int semb_plan_run(semb_plan* plan);
+
+/* Copy the results to host arrays of ncdps*ns elements, CDP-major in the gather's
+ * CDP order: ctr = picked candidate index (CMP: -1 when no candidate has positive
+ * semblance; CRS: linear index ia*nb*nc + ib*nc + ic), str = semblance, stk = stack.
+ * These are the reference's ctr/str/stk arrays (CRS/OpenMP/src/main.cpp:126-128). */
+int semb_plan_download(semb_plan* plan, int32_t* ctr, float* str, float* stk);
+
+/* Copy the device-built neighbour lists (CRS): off[ncdps+1], list[off[ncdps]]
+ * (pass list = NULL to query the size in *n_out).  The lists are those of
+ * su_gather::su_gather (CRS/OpenMP/src/su_gather.cpp:70-87). */
+int semb_plan_neighbours(semb_plan* plan, int32_t* off, int32_t* list, int64_t* n_out);
+
+typedef struct semb_stats {
+  double ms_search;       /* device time of the last run's semblance kernel(s) */
+  double ms_repick;       /* device time of the last run's FP64 re-pick kernel */
+  double ms_total;        /* device time of the whole last run */
+  double ms_upload;       /* device time of the last upload (copies + binning) */
+  int64_t evals;          /* (CDP, t0, candidate) semblance evaluations per run */
+  int64_t trace_evals;    /* evals x aperture traces (the reference's "semblance-traces") */
+  int64_t repicked;       /* (CDP, t0) pairs re-evaluated in FP64 by the last run */
+  int64_t kernel_launches;/* kernels launched by the last run */
+  int32_t window;         /* w = 2*tau+1 */
+  int32_t max_aperture;   /* largest aperture (traces) */
+  int32_t ncdps, ns, ncand;
+  int32_t grid_ctas;      /* CTAs of the main search launch */
+  int32_t ctas_per_sm;    /* resident CTAs per SM of the main search kernel */
+  int32_t sms;
+} semb_stats;
+
+int semb_plan_stats(const semb_plan* plan, semb_stats* out);
+
+/* Capture the search (work-queue reset + kernels) in a CUDA graph and replay it on
+ * later semb_plan_run calls (batched form).  on = 0 goes back to direct launches. */
+int semb_plan_use_graph(semb_plan* plan, int32_t on);
+
+int semb_plan_destroy(semb_plan* plan);
+
+/* ---- helpers ---------------------------------------------------------------- */
+
+/* Page-locked host memory for input/output buffers (cudaMallocHost). */
+int semb_host_alloc(size_t bytes, void** out);
+int semb_host_free(void* p);
+
+/* Number of visible CUDA devices (0 when none); never fails. */
+int32_t semb_device_count(void);
+
+const char* semb_strerror(int code);
+const char* semb_last_error(void);
+int32_t semb_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEMB_GB300_H */

@@ -1,0 +1,69 @@
+// Kernel lookup and launch helpers shared by the plan.
+#include <cuda_runtime.h>
+
+#include "common.h"
+#include "plan_kernels.cuh"
+#include "search_inst.cuh"
+
+namespace semb {
+
+SearchEntry search_entry_cmp_plain(int w);
+SearchEntry search_entry_cmp_fast(int w);
+SearchEntry search_entry_crs_plain(int w);
+SearchEntry search_entry_crs_fast(int w);
+
+static SearchEntry lookup(int method, int form, int w) {
+  if (method == METHOD_CMP) return form == FORM_PLAIN ? search_entry_cmp_plain(w) : search_entry_cmp_fast(w);
+  return form == FORM_PLAIN ? search_entry_crs_plain(w) : search_entry_crs_fast(w);
+}
+
+int search_rc(int method, int form, int w) { return lookup(method, form, w).rc; }
+
+int search_occupancy(int method, int form, int w, int nwarps, size_t smem, int* ctas_per_sm) {
+  SearchEntry e = lookup(method, form, w);
+  if (!e.fn) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", w);
+  SEMB_CUDA(cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SEMB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, e.fn, nwarps * 32, smem));
+  return SEMB_OK;
+}
+
+int launch_search(int method, int form, int w, const KParams& P, int nwarps, int grid, size_t smem,
+                  cudaStream_t st) {
+  SearchEntry e = lookup(method, form, w);
+  if (!e.fn) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", w);
+  void* args[] = {const_cast<KParams*>(&P)};
+  SEMB_CUDA(cudaLaunchKernel(e.fn, dim3(grid), dim3(nwarps * 32), args, smem, st));
+  return SEMB_OK;
+}
+
+int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st) {
+  const int grid = (ncdps + 127) / 128;
+  switch (w) {
+    case 1: k_crs_stt00<1><<<grid, 128, 0, st>>>(ncdps, P, a, b, c, out); break;
+    case 3: k_crs_stt00<3><<<grid, 128, 0, st>>>(ncdps, P, a, b, c, out); break;
+    case 5: k_crs_stt00<5><<<grid, 128, 0, st>>>(ncdps, P, a, b, c, out); break;
+    default: return fail(SEMB_E_WINDOW, "no CRS kernel for w = %d", w);
+  }
+  SEMB_CUDA(cudaGetLastError());
+  return SEMB_OK;
+}
+
+int launch_repick(int w, const RepickParams& R, cudaStream_t st) {
+  const int64_t items = (int64_t)R.ncdps * R.ns;
+  const int grid = (int)((items + 7) / 8);
+  switch (w) {
+    case 1: k_repick<1><<<grid, 256, 0, st>>>(R); break;
+    case 3: k_repick<3><<<grid, 256, 0, st>>>(R); break;
+    case 5: k_repick<5><<<grid, 256, 0, st>>>(R); break;
+    case 7: k_repick<7><<<grid, 256, 0, st>>>(R); break;
+    case 9: k_repick<9><<<grid, 256, 0, st>>>(R); break;
+    case 11: k_repick<11><<<grid, 256, 0, st>>>(R); break;
+    case 13: k_repick<13><<<grid, 256, 0, st>>>(R); break;
+    case 15: k_repick<15><<<grid, 256, 0, st>>>(R); break;
+    default: return fail(SEMB_E_WINDOW, "no re-pick kernel for w = %d", w);
+  }
+  SEMB_CUDA(cudaGetLastError());
+  return SEMB_OK;
+}
+
+}  // namespace semb

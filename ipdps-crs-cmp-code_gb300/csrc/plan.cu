@@ -1,0 +1,766 @@
+// semb_plan: device state and the C ABI of the search (see include/semb_gb300.h).
+//
+// Device data layout (all in HBM, built once per upload):
+//   samples    FP32 [ntraces][pitch], pitch = ns rounded up to 8 (16-byte rows)
+//   samples16  FP16/BF16 [ntraces][pitch] + scale[ntraces]   (batched form)
+//   ap_off     int64 [ncdps+1]; ap_tr int32, ap_geo float4 (|dm|, dm^2, h, -),
+//              ap_geo64 (double |dm|, dm^2, h) per aperture entry
+//   cand       float4 [npass*cpp]: candidates in search order (C-major for CRS)
+//   tasks      int2 (cdp, t0_start), sorted by decreasing aperture
+//   outputs    ctr/str/stk [ncdps][ns]; top-4 [ncdps][ns][4] (batched form)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "common.h"
+#include "plan_kernels.cuh"
+#include "semb_kernels.cuh"
+
+namespace semb {
+
+// Launchers of the search kernel instantiations (kernels_*.cu).
+int launch_search(int method, int form, int w, const KParams& P, int nwarps, int grid, size_t smem,
+                  cudaStream_t st);
+int search_rc(int method, int form, int w);
+int search_occupancy(int method, int form, int w, int nwarps, size_t smem, int* ctas_per_sm);
+int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
+int launch_repick(int w, const RepickParams& R, cudaStream_t st);
+
+}  // namespace semb
+
+using namespace semb;
+
+struct semb_plan {
+  semb_params p{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sms = 0;
+  bool uploaded = false;
+
+  int ncdps = 0, ns = 0, dt_us = 0;
+  int64_t ntraces = 0, pitch = 0, nap = 0;
+  float dt = 0.f, idt = 0.f;
+  double dt64 = 0.0, idt64 = 0.0;
+  int tau = 0, w = 1;
+  int ncand = 0, npass = 0, cpp = 0, nwarps = 0, rc = 0;
+  int ntasks = 0, max_ap = 0;
+  size_t smem = 0;
+  int cap = 0;
+  int grid = 0, ctas_per_sm = 0;
+  int64_t n_nbr = 0;
+  float cand0_a = 0.f, cand0_b = 0.f, cand0_c = 0.f;
+
+  // device buffers
+  float* d_samples = nullptr;
+  uint16_t* d_samples16 = nullptr;
+  float* d_scale = nullptr;
+  int64_t* d_ap_off = nullptr;
+  int32_t* d_ap_tr = nullptr;
+  float4* d_ap_geo = nullptr;
+  Geo64* d_ap_geo64 = nullptr;
+  int64_t* d_nbr_off = nullptr;
+  int32_t* d_nbr = nullptr;
+  float4* d_cand = nullptr;
+  float* d_pass_bounds = nullptr;
+  double* d_cand64 = nullptr;
+  int2* d_tasks = nullptr;
+  int* d_counter = nullptr;
+  int32_t* d_ctr = nullptr;
+  float* d_str = nullptr;
+  float* d_stk = nullptr;
+  float* d_stt00 = nullptr;
+  float* d_top_sem = nullptr;
+  int32_t* d_top_idx = nullptr;
+  float* d_top_stk = nullptr;
+  int* d_status = nullptr;
+  unsigned long long* d_repicked = nullptr;
+
+  cudaEvent_t ev[6] = {};
+  bool use_graph = false;
+  cudaGraphExec_t graph = nullptr;
+  semb_stats stats{};
+};
+
+namespace {
+
+template <typename T>
+int dev_alloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  if (e != cudaSuccess)
+    return fail(SEMB_E_NOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+  return SEMB_OK;
+}
+
+// Device scratch freed when the guard goes out of scope (all exit paths).
+struct Scratch {
+  std::vector<void*> ptrs;
+  ~Scratch() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  int alloc(T** p, size_t n) {
+    int rc = dev_alloc(p, n);
+    if (rc == SEMB_OK) ptrs.push_back(*p);
+    return rc;
+  }
+};
+
+template <typename T>
+void dev_free(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+void free_data(semb_plan* pl) {
+  dev_free(pl->d_samples);
+  dev_free(pl->d_samples16);
+  dev_free(pl->d_scale);
+  dev_free(pl->d_ap_off);
+  dev_free(pl->d_ap_tr);
+  dev_free(pl->d_ap_geo);
+  dev_free(pl->d_ap_geo64);
+  dev_free(pl->d_nbr_off);
+  dev_free(pl->d_nbr);
+  dev_free(pl->d_cand);
+  dev_free(pl->d_pass_bounds);
+  dev_free(pl->d_cand64);
+  dev_free(pl->d_tasks);
+  dev_free(pl->d_ctr);
+  dev_free(pl->d_str);
+  dev_free(pl->d_stk);
+  dev_free(pl->d_stt00);
+  dev_free(pl->d_top_sem);
+  dev_free(pl->d_top_idx);
+  dev_free(pl->d_top_stk);
+  if (pl->graph) cudaGraphExecDestroy(pl->graph);
+  pl->graph = nullptr;
+  pl->uploaded = false;
+}
+
+int check_params(const semb_params* p) {
+  if (!p) return fail(SEMB_E_ARG, "null params");
+  if (p->method != SEMB_CMP && p->method != SEMB_CRS) return fail(SEMB_E_ARG, "unknown method %d", p->method);
+  if (p->mode != SEMB_PLAIN_F32 && p->mode != SEMB_BATCHED) return fail(SEMB_E_ARG, "unknown mode %d", p->mode);
+  if (p->nc <= 0) return fail(SEMB_E_ARG, "nc must be positive");
+  if (p->method == SEMB_CRS && (p->na <= 0 || p->nb <= 0)) return fail(SEMB_E_ARG, "na and nb must be positive");
+  const int64_t ncand = p->method == SEMB_CMP ? (int64_t)p->nc : (int64_t)p->na * p->nb * p->nc;
+  if (ncand > (1 << 24)) return fail(SEMB_E_ARG, "candidate grid of %lld is too large", (long long)ncand);
+  if (p->storage < SEMB_STORE_F32 || p->storage > SEMB_STORE_BF16) return fail(SEMB_E_ARG, "unknown storage");
+  if (p->repick < 0 || p->repick > 2) return fail(SEMB_E_ARG, "unknown repick mode");
+  if (!(p->tau >= 0.0) || !std::isfinite(p->tau)) return fail(SEMB_E_ARG, "tau must be a non-negative number");
+  return SEMB_OK;
+}
+
+// Reference parameter grids.  Single precision: the reference's float build
+// (CMP/OpenMP/src/main.cpp:88,119-122; CRS/OpenMP/src/main.cpp:112-116,155-160
+// with real = float); double precision: its double build.  `volatile` keeps each
+// operation rounded on its own whatever the host compiler's contraction rules.
+void grid_f32(const semb_params& p, std::vector<float>& a, std::vector<float>& b, std::vector<float>& c) {
+  if (p.method == SEMB_CMP) {
+    const int nc = p.nc;
+    const float c0 = (float)(p.c0 * kFactor), c1 = (float)(p.c1 * kFactor);
+    volatile float diff = c1 - c0;
+    const float inc = diff * (1.0f / (float)nc);
+    a.assign(nc, 0.f);
+    b.assign(nc, 0.f);
+    c.resize(nc);
+    for (int i = 0; i < nc; ++i) {
+      volatile float prod = inc * (float)i;
+      c[i] = c0 + prod;
+    }
+  } else {
+    const int na = p.na, nb = p.nb, nc = p.nc, n = na * nb * nc;
+    const float a0 = (float)p.a0, a1 = (float)p.a1, b0 = (float)p.b0, b1 = (float)p.b1;
+    const float c0 = (float)(p.c0 * kFactor), c1 = (float)(p.c1 * kFactor);
+    volatile float da = a1 - a0, db = b1 - b0, dc = c1 - c0;
+    const float inc_a = (float)((double)da * (1.0 / (double)(float)na));
+    const float inc_b = (float)((double)db * (1.0 / (double)(float)nb));
+    const float inc_c = (float)((double)dc * (1.0 / (double)(float)nc));
+    a.resize(n);
+    b.resize(n);
+    c.resize(n);
+    for (int i = 0; i < n; ++i) {
+      volatile float pa = inc_a * (float)(i / (nc * nb));
+      volatile float pb = inc_b * (float)((i / nc) % nb);
+      volatile float pc = inc_c * (float)(i % nc);
+      a[i] = a0 + pa;
+      b[i] = b0 + pb;
+      c[i] = c0 + pc;
+    }
+  }
+}
+
+void grid_f64(const semb_params& p, std::vector<double>& abc) {
+  if (p.method == SEMB_CMP) {
+    const int nc = p.nc;
+    const double c0 = p.c0 * kFactor, c1 = p.c1 * kFactor;
+    const double inc = (c1 - c0) * (1.0 / (double)nc);
+    abc.assign(3 * (size_t)nc, 0.0);
+    for (int i = 0; i < nc; ++i) {
+      volatile double prod = inc * (double)i;
+      abc[3 * i + 2] = c0 + prod;
+    }
+  } else {
+    const int na = p.na, nb = p.nb, nc = p.nc, n = na * nb * nc;
+    const double a0 = p.a0, b0 = p.b0, c0 = p.c0 * kFactor;
+    const double inc_a = (p.a1 - a0) * (1.0 / (double)na);
+    const double inc_b = (p.b1 - b0) * (1.0 / (double)nb);
+    const double inc_c = (p.c1 * kFactor - c0) * (1.0 / (double)nc);
+    abc.resize(3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+      volatile double pa = inc_a * (double)(i / (nc * nb));
+      volatile double pb = inc_b * (double)((i / nc) % nb);
+      volatile double pc = inc_c * (double)(i % nc);
+      abc[3 * (size_t)i] = a0 + pa;
+      abc[3 * (size_t)i + 1] = b0 + pb;
+      abc[3 * (size_t)i + 2] = c0 + pc;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t semb_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int semb_host_alloc(size_t bytes, void** out) {
+  if (!out) return fail(SEMB_E_ARG, "null argument");
+  *out = nullptr;
+  SEMB_CUDA(cudaMallocHost(out, bytes ? bytes : 1));
+  return SEMB_OK;
+}
+
+int semb_host_free(void* p) {
+  if (p) SEMB_CUDA(cudaFreeHost(p));
+  return SEMB_OK;
+}
+
+int semb_plan_create(const semb_params* p, int32_t device, semb_plan** out) {
+  if (!out) return fail(SEMB_E_ARG, "null argument");
+  *out = nullptr;
+  SEMB_TRY(check_params(p));
+  if (semb_device_count() <= device || device < 0)
+    return fail(SEMB_E_NODEV, "CUDA device %d is not available", device);
+  SEMB_CUDA(cudaSetDevice(device));
+  semb_plan* pl = new (std::nothrow) semb_plan();
+  if (!pl) return fail(SEMB_E_NOMEM, "out of host memory");
+  pl->p = *p;
+  pl->device = device;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&pl->ev[i]);
+  if (e == cudaSuccess) e = cudaMalloc(&pl->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&pl->d_counter, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&pl->d_repicked, sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    semb_plan_destroy(pl);
+    return fail(SEMB_E_CUDA, "plan set-up failed: %s", cudaGetErrorString(e));
+  }
+  if (prop.major < 10) {
+    semb_plan_destroy(pl);
+    return fail(SEMB_E_NODEV, "device %d is sm_%d%d; this library is built for sm_103a", device, prop.major,
+                prop.minor);
+  }
+  pl->sms = prop.multiProcessorCount;
+  *out = pl;
+  return SEMB_OK;
+}
+
+int semb_plan_destroy(semb_plan* pl) {
+  if (!pl) return SEMB_OK;
+  cudaSetDevice(pl->device);
+  if (pl->stream) cudaStreamSynchronize(pl->stream);
+  free_data(pl);
+  dev_free(pl->d_status);
+  dev_free(pl->d_counter);
+  dev_free(pl->d_repicked);
+  for (auto& ev : pl->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (pl->stream) cudaStreamDestroy(pl->stream);
+  delete pl;
+  return SEMB_OK;
+}
+
+int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
+  if (!pl || !g) return fail(SEMB_E_ARG, "null argument");
+  const semb_params& p = pl->p;
+  if (g->ncdps <= 0 || g->ns <= 0 || g->ntraces <= 0 || !g->cdp_end || !g->gx || !g->gy || !g->sx || !g->sy ||
+      !g->scalco || !g->samples)
+    return fail(SEMB_E_ARG, "empty or incomplete gather");
+  if (g->ns > 65535) return fail(SEMB_E_ARG, "ns %d exceeds the SU limit", g->ns);
+  if (g->dt_us <= 0) return fail(SEMB_E_ARG, "dt must be positive");
+  if (g->ntraces >= (int64_t)1 << 31) return fail(SEMB_E_ARG, "more than 2^31 traces");
+  int64_t prev = 0;
+  for (int i = 0; i < g->ncdps; ++i) {
+    if (g->cdp_end[i] <= prev) return fail(SEMB_E_ARG, "CDP %d has no traces (cdp_end must increase)", i);
+    prev = g->cdp_end[i];
+  }
+  if (prev != g->ntraces) return fail(SEMB_E_ARG, "cdp_end[ncdps-1] must equal ntraces");
+
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  free_data(pl);
+  cudaStream_t st = pl->stream;
+  pl->ncdps = g->ncdps;
+  pl->ns = g->ns;
+  pl->dt_us = g->dt_us;
+  pl->ntraces = g->ntraces;
+  pl->pitch = (g->ns + 7) & ~7;
+
+  // time sampling (CMP/OpenMP/src/main.cpp:107-110, CRS/OpenMP/src/main.cpp:135-138)
+  {
+    volatile float dt = (float)g->dt_us;
+    dt = dt / 1000000.0f;
+    const float idt = 1.0f / dt;
+    const float itau = (float)p.tau;
+    volatile float prod = itau * idt;
+    const int tau = (int)prod > 0 ? (int)prod : 0;
+    pl->dt = dt;
+    pl->idt = idt;
+    pl->tau = tau;
+    pl->w = 2 * tau + 1;
+    pl->dt64 = (double)g->dt_us / 1000000.0f;
+    pl->idt64 = 1.0f / pl->dt64;
+  }
+  const int maxw = p.method == SEMB_CMP ? kMaxWCmp : kMaxWCrs;
+  if (pl->w > maxw)
+    return fail(SEMB_E_WINDOW, "semblance window w = %d exceeds the maximum %d of this method", pl->w, maxw);
+
+  cudaEventRecord(pl->ev[4], st);
+  // trace store
+  const int64_t ntr = g->ntraces;
+  SEMB_TRY(dev_alloc(&pl->d_samples, (size_t)ntr * pl->pitch));
+  SEMB_CUDA(cudaMemsetAsync(pl->d_samples, 0, (size_t)ntr * pl->pitch * sizeof(float), st));
+  SEMB_CUDA(cudaMemcpy2DAsync(pl->d_samples, pl->pitch * sizeof(float), g->samples, (size_t)g->ns * sizeof(float),
+                              (size_t)g->ns * sizeof(float), (size_t)ntr, cudaMemcpyHostToDevice, st));
+
+  // header fields and CDP ranges (scratch for the set-up kernels)
+  int32_t *d_gx, *d_gy, *d_sx, *d_sy, *d_sc;
+  int64_t* d_cdp_end;
+  float *d_h32, *d_mx32, *d_my32, *d_fmx, *d_fmy;
+  double *d_h64, *d_mx64, *d_my64;
+  int32_t* d_cnt32;
+  int64_t* d_cnt64;
+  Scratch scratch;
+  SEMB_TRY(scratch.alloc(&d_gx, ntr));
+  SEMB_TRY(scratch.alloc(&d_gy, ntr));
+  SEMB_TRY(scratch.alloc(&d_sx, ntr));
+  SEMB_TRY(scratch.alloc(&d_sy, ntr));
+  SEMB_TRY(scratch.alloc(&d_sc, ntr));
+  SEMB_TRY(scratch.alloc(&d_cdp_end, g->ncdps));
+  SEMB_TRY(scratch.alloc(&d_h32, ntr));
+  SEMB_TRY(scratch.alloc(&d_mx32, ntr));
+  SEMB_TRY(scratch.alloc(&d_my32, ntr));
+  SEMB_TRY(scratch.alloc(&d_h64, ntr));
+  SEMB_TRY(scratch.alloc(&d_mx64, ntr));
+  SEMB_TRY(scratch.alloc(&d_my64, ntr));
+  SEMB_TRY(scratch.alloc(&d_fmx, g->ncdps));
+  SEMB_TRY(scratch.alloc(&d_fmy, g->ncdps));
+  SEMB_TRY(scratch.alloc(&d_cnt32, g->ncdps));
+  SEMB_TRY(scratch.alloc(&d_cnt64, g->ncdps));
+  SEMB_CUDA(cudaMemcpyAsync(d_gx, g->gx, ntr * 4, cudaMemcpyHostToDevice, st));
+  SEMB_CUDA(cudaMemcpyAsync(d_gy, g->gy, ntr * 4, cudaMemcpyHostToDevice, st));
+  SEMB_CUDA(cudaMemcpyAsync(d_sx, g->sx, ntr * 4, cudaMemcpyHostToDevice, st));
+  SEMB_CUDA(cudaMemcpyAsync(d_sy, g->sy, ntr * 4, cudaMemcpyHostToDevice, st));
+  SEMB_CUDA(cudaMemcpyAsync(d_sc, g->scalco, ntr * 4, cudaMemcpyHostToDevice, st));
+  SEMB_CUDA(cudaMemcpyAsync(d_cdp_end, g->cdp_end, g->ncdps * 8, cudaMemcpyHostToDevice, st));
+
+  const int tgrid = (int)std::min<int64_t>((ntr + 255) / 256, 65535);
+  k_trace_geometry<<<tgrid, 256, 0, st>>>(ntr, d_gx, d_gy, d_sx, d_sy, d_sc, d_h32, d_mx32, d_my32, d_h64, d_mx64,
+                                          d_my64);
+  SEMB_CUDA(cudaGetLastError());
+
+  // neighbour lists: CRS from midpoints within apm, CMP the CDP itself
+  const int nc_blocks = (g->ncdps + 255) / 256;
+  SEMB_TRY(dev_alloc(&pl->d_nbr_off, g->ncdps + 1));
+  if (p.method == SEMB_CRS) {
+    k_cdp_midpoints<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_cdp_end, d_gx, d_gy, d_sx, d_sy, d_sc, d_fmx, d_fmy);
+    const float lim = (float)((int32_t)p.apm * (int32_t)p.apm);
+    k_neighbours<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_fmx, d_fmy, lim, d_cnt32, nullptr, nullptr);
+    k_scan_exclusive<int32_t><<<1, 1024, 0, st>>>(g->ncdps, d_cnt32, pl->d_nbr_off);
+    SEMB_CUDA(cudaMemcpyAsync(&pl->n_nbr, pl->d_nbr_off + g->ncdps, 8, cudaMemcpyDeviceToHost, st));
+    SEMB_CUDA(cudaStreamSynchronize(st));
+    SEMB_TRY(dev_alloc(&pl->d_nbr, (size_t)pl->n_nbr));
+    k_neighbours<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_fmx, d_fmy, lim, nullptr, pl->d_nbr_off, pl->d_nbr);
+  } else {
+    std::vector<int64_t> off(g->ncdps + 1);
+    std::vector<int32_t> lst(g->ncdps);
+    for (int i = 0; i <= g->ncdps; ++i) off[i] = i;
+    std::iota(lst.begin(), lst.end(), 0);
+    pl->n_nbr = g->ncdps;
+    SEMB_TRY(dev_alloc(&pl->d_nbr, g->ncdps));
+    SEMB_CUDA(cudaMemcpyAsync(pl->d_nbr_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice, st));
+    SEMB_CUDA(cudaMemcpyAsync(pl->d_nbr, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice, st));
+    SEMB_CUDA(cudaStreamSynchronize(st));
+  }
+  SEMB_CUDA(cudaGetLastError());
+
+  // aperture lists
+  SEMB_TRY(dev_alloc(&pl->d_ap_off, g->ncdps + 1));
+  k_aperture_count<<<nc_blocks, 256, 0, st>>>(g->ncdps, pl->d_nbr_off, pl->d_nbr, d_cdp_end, d_cnt64);
+  k_scan_exclusive<int64_t><<<1, 1024, 0, st>>>(g->ncdps, d_cnt64, pl->d_ap_off);
+  std::vector<int64_t> ap_off(g->ncdps + 1);
+  SEMB_CUDA(cudaMemcpyAsync(ap_off.data(), pl->d_ap_off, ap_off.size() * 8, cudaMemcpyDeviceToHost, st));
+  SEMB_CUDA(cudaStreamSynchronize(st));
+  pl->nap = ap_off[g->ncdps];
+  SEMB_TRY(dev_alloc(&pl->d_ap_tr, pl->nap));
+  SEMB_TRY(dev_alloc(&pl->d_ap_geo, pl->nap));
+  SEMB_TRY(dev_alloc(&pl->d_ap_geo64, pl->nap));
+  k_aperture_fill<<<(g->ncdps + 7) / 8, 256, 0, st>>>(g->ncdps, p.method, pl->d_nbr_off, pl->d_nbr, d_cdp_end,
+                                                       pl->d_ap_off, d_h32, d_mx32, d_my32, d_h64, d_mx64, d_my64,
+                                                       pl->d_ap_tr, pl->d_ap_geo, pl->d_ap_geo64);
+  SEMB_CUDA(cudaGetLastError());
+  int max_ap = 0;
+  for (int i = 0; i < g->ncdps; ++i) max_ap = std::max<int64_t>(max_ap, ap_off[i + 1] - ap_off[i]);
+  pl->max_ap = max_ap;
+
+  // 16-bit store (batched form)
+  if (p.mode == SEMB_BATCHED && p.storage != SEMB_STORE_F32) {
+    SEMB_TRY(dev_alloc(&pl->d_samples16, (size_t)ntr * pl->pitch));
+    SEMB_TRY(dev_alloc(&pl->d_scale, ntr));
+    k_make_store16<<<(int)std::min<int64_t>(ntr, 65535), 256, 0, st>>>(ntr, g->ns, pl->pitch, p.storage,
+                                                                       pl->d_samples, pl->d_samples16, pl->d_scale);
+    SEMB_CUDA(cudaGetLastError());
+  }
+
+  // candidate grid, search order and passes
+  std::vector<float> ga, gb, gc;
+  grid_f32(p, ga, gb, gc);
+  std::vector<double> g64;
+  grid_f64(p, g64);
+  const int ncand = (int)gc.size();
+  pl->ncand = ncand;
+  pl->cand0_a = ga[0];
+  pl->cand0_b = gb[0];
+  pl->cand0_c = gc[0];
+  std::vector<int> order(ncand);
+  if (p.method == SEMB_CMP) {
+    std::iota(order.begin(), order.end(), 0);
+  } else {
+    // C outermost, then A, then B: a pass spans few C values, which dominate the
+    // spread of traveltimes, so its staged windows stay narrow.
+    int q = 0;
+    for (int ic = 0; ic < p.nc; ++ic)
+      for (int ia = 0; ia < p.na; ++ia)
+        for (int ib = 0; ib < p.nb; ++ib) order[q++] = ia * p.nb * p.nc + ib * p.nc + ic;
+  }
+  const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
+  const int rc = search_rc(p.method, form, pl->w);
+  if (rc <= 0) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", pl->w);
+  int best_nw = 8, best_tot = INT32_MAX;
+  for (int nw = 8; nw >= 4; --nw) {
+    const int per = nw * rc;
+    const int tot = ((ncand + per - 1) / per) * per;
+    if (tot < best_tot) {
+      best_tot = tot;
+      best_nw = nw;
+    }
+  }
+  pl->nwarps = best_nw;
+  pl->rc = rc;
+  pl->cpp = best_nw * rc;
+  pl->npass = (ncand + pl->cpp - 1) / pl->cpp;
+  const int npad = pl->npass * pl->cpp;
+  std::vector<float4> cand(npad);
+  std::vector<float> bounds((size_t)pl->npass * 8, 0.f);
+  const double s1 = pl->idt64, s2 = pl->idt64 * pl->idt64;
+  for (int k = 0; k < npad; ++k) {
+    const int gi = order[std::min(k, ncand - 1)];
+    float4 v;
+    if (form == FORM_PLAIN) {
+      v = make_float4(ga[gi], gb[gi], gc[gi], 0.f);
+    } else {
+      v = make_float4((float)(g64[3 * (size_t)gi] * s1), (float)(g64[3 * (size_t)gi + 1] * s2),
+                      (float)(g64[3 * (size_t)gi + 2] * s2), 0.f);
+    }
+    int32_t gbits = gi;
+    std::memcpy(&v.w, &gbits, 4);
+    cand[k] = v;
+    float* bp = &bounds[(size_t)(k / pl->cpp) * 8];
+    if (k % pl->cpp == 0) {
+      bp[0] = bp[1] = ga[gi];
+      bp[2] = bp[3] = gb[gi];
+      bp[4] = bp[5] = gc[gi];
+    } else {
+      bp[0] = std::min(bp[0], ga[gi]);
+      bp[1] = std::max(bp[1], ga[gi]);
+      bp[2] = std::min(bp[2], gb[gi]);
+      bp[3] = std::max(bp[3], gb[gi]);
+      bp[4] = std::min(bp[4], gc[gi]);
+      bp[5] = std::max(bp[5], gc[gi]);
+    }
+  }
+  SEMB_TRY(dev_alloc(&pl->d_cand, npad));
+  SEMB_TRY(dev_alloc(&pl->d_pass_bounds, bounds.size()));
+  SEMB_TRY(dev_alloc(&pl->d_cand64, g64.size()));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_cand, cand.data(), npad * sizeof(float4), cudaMemcpyHostToDevice, st));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_pass_bounds, bounds.data(), bounds.size() * 4, cudaMemcpyHostToDevice, st));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_cand64, g64.data(), g64.size() * 8, cudaMemcpyHostToDevice, st));
+
+  // work queue: (cdp, t0 block), largest aperture first (longest-processing-time order)
+  const int nblk = (g->ns + kTB - 1) / kTB;
+  std::vector<int> cdp_order(g->ncdps);
+  std::iota(cdp_order.begin(), cdp_order.end(), 0);
+  std::stable_sort(cdp_order.begin(), cdp_order.end(), [&](int x, int y) {
+    return ap_off[x + 1] - ap_off[x] > ap_off[y + 1] - ap_off[y];
+  });
+  const int64_t ntasks = (int64_t)g->ncdps * nblk;
+  if (ntasks >= INT32_MAX) return fail(SEMB_E_ARG, "too many tasks");
+  std::vector<int2> tasks((size_t)ntasks);
+  size_t q = 0;
+  for (int c : cdp_order)
+    for (int b = 0; b < nblk; ++b) tasks[q++] = make_int2(c, b * kTB);
+  pl->ntasks = (int)ntasks;
+  SEMB_TRY(dev_alloc(&pl->d_tasks, tasks.size()));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_tasks, tasks.data(), tasks.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+
+  // outputs
+  const size_t nout = (size_t)g->ncdps * g->ns;
+  SEMB_TRY(dev_alloc(&pl->d_ctr, nout));
+  SEMB_TRY(dev_alloc(&pl->d_str, nout));
+  SEMB_TRY(dev_alloc(&pl->d_stk, nout));
+  SEMB_TRY(dev_alloc(&pl->d_stt00, g->ncdps));
+  SEMB_CUDA(cudaMemsetAsync(pl->d_stt00, 0, g->ncdps * sizeof(float), st));
+  if (form == FORM_FAST) {
+    SEMB_TRY(dev_alloc(&pl->d_top_sem, nout * kTopK));
+    SEMB_TRY(dev_alloc(&pl->d_top_idx, nout * kTopK));
+    SEMB_TRY(dev_alloc(&pl->d_top_stk, nout * kTopK));
+  }
+
+  // staging capacity: as large as two resident CTAs per SM allow, at least one trace
+  const size_t fixed = 64 + ((sizeof(ChunkMeta) + 127) / 128) * 128 + kMaxChunk * sizeof(int4);
+  int cap = 24576;
+  cap = std::max<int>(cap, (int)pl->pitch + 16);
+  cap = (cap + 7) & ~7;
+  pl->cap = cap;
+  pl->smem = fixed + (size_t)cap * sizeof(float);
+  if (pl->smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", g->ns);
+  SEMB_TRY(search_occupancy(p.method, form, pl->w, pl->nwarps, pl->smem, &pl->ctas_per_sm));
+  if (pl->ctas_per_sm <= 0) return fail(SEMB_E_CUDA, "search kernel cannot be resident with %zu bytes", pl->smem);
+  pl->grid = form == FORM_PLAIN ? pl->ntasks : std::min(pl->ntasks, pl->sms * pl->ctas_per_sm);
+  cudaEventRecord(pl->ev[5], st);
+  SEMB_CUDA(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, pl->ev[4], pl->ev[5]);
+
+
+  std::memset(&pl->stats, 0, sizeof(pl->stats));
+  pl->stats.ms_upload = ms;
+  pl->stats.window = pl->w;
+  pl->stats.max_aperture = pl->max_ap;
+  pl->stats.ncdps = pl->ncdps;
+  pl->stats.ns = pl->ns;
+  pl->stats.ncand = pl->ncand;
+  pl->stats.evals = (int64_t)pl->ncdps * pl->ns * pl->ncand;
+  pl->stats.trace_evals = pl->nap * (int64_t)pl->ns * pl->ncand;
+  pl->stats.grid_ctas = pl->grid;
+  pl->stats.ctas_per_sm = pl->ctas_per_sm;
+  pl->stats.sms = pl->sms;
+  pl->uploaded = true;
+  return SEMB_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+KParams make_kparams(semb_plan* pl) {
+  KParams P{};
+  P.samples = pl->d_samples;
+  P.samples16 = pl->d_samples16;
+  P.scale = pl->d_scale;
+  P.pitch = pl->pitch;
+  P.storage = (pl->p.mode == SEMB_BATCHED) ? pl->p.storage : SEMB_STORE_F32;
+  P.ap_off = pl->d_ap_off;
+  P.ap_tr = pl->d_ap_tr;
+  P.ap_geo = pl->d_ap_geo;
+  P.cand = pl->d_cand;
+  P.pass_bounds = pl->d_pass_bounds;
+  P.npass = pl->npass;
+  P.cpp = pl->cpp;
+  P.tasks = pl->d_tasks;
+  P.ntasks = pl->ntasks;
+  P.counter = pl->d_counter;
+  P.ns = pl->ns;
+  P.tau = pl->tau;
+  P.dt = pl->dt;
+  P.idt = pl->idt;
+  P.cap = pl->cap;
+  P.ctr = pl->d_ctr;
+  P.str = pl->d_str;
+  P.stk = pl->d_stk;
+  P.stt00 = pl->d_stt00;
+  P.top_sem = pl->d_top_sem;
+  P.top_idx = pl->d_top_idx;
+  P.top_stk = pl->d_top_stk;
+  P.status = pl->d_status;
+  return P;
+}
+
+// Enqueue one whole search on the plan's stream (no synchronization).
+int enqueue_run(semb_plan* pl, bool timed) {
+  cudaStream_t st = pl->stream;
+  const semb_params& p = pl->p;
+  const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
+  KParams P = make_kparams(pl);
+  int launches = 0;
+  if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[0], st));
+  if (pl->ns < 2 * pl->tau + 2) {
+    // no trace can hold a whole window: every item is out of range
+    SEMB_CUDA(cudaMemsetAsync(pl->d_str, 0, (size_t)pl->ncdps * pl->ns * 4, st));
+    SEMB_CUDA(cudaMemsetAsync(pl->d_stk, 0, (size_t)pl->ncdps * pl->ns * 4, st));
+    SEMB_CUDA(cudaMemsetAsync(pl->d_ctr, p.method == SEMB_CMP ? 0xff : 0, (size_t)pl->ncdps * pl->ns * 4, st));
+    if (timed) {
+      SEMB_CUDA(cudaEventRecord(pl->ev[1], st));
+      SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
+      SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
+    }
+    pl->stats.kernel_launches = 0;
+    return SEMB_OK;
+  }
+  if (p.method == SEMB_CRS) {
+    SEMB_TRY(launch_stt00(pl->w, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
+    ++launches;
+  }
+  if (form == FORM_FAST) SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st));
+  if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[1], st));
+  SEMB_TRY(launch_search(p.method, form, pl->w, P, pl->nwarps, pl->grid, pl->smem, st));
+  ++launches;
+  if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
+  if (form == FORM_FAST) {
+    RepickParams R{};
+    R.top_sem = pl->d_top_sem;
+    R.top_idx = pl->d_top_idx;
+    R.top_stk = pl->d_top_stk;
+    R.samples = pl->d_samples;
+    R.pitch = pl->pitch;
+    R.ap_off = pl->d_ap_off;
+    R.ap_tr = pl->d_ap_tr;
+    R.ap_geo64 = pl->d_ap_geo64;
+    R.cand64 = pl->d_cand64;
+    R.stt00 = pl->d_stt00;
+    R.ncdps = pl->ncdps;
+    R.ns = pl->ns;
+    R.tau = pl->tau;
+    R.method = p.method;
+    R.mode = p.repick;
+    R.dt = pl->dt64;
+    R.idt = pl->idt64;
+    R.gap = p.repick_gap;
+    R.ctr = pl->d_ctr;
+    R.str = pl->d_str;
+    R.stk = pl->d_stk;
+    R.repicked = pl->d_repicked;
+    SEMB_CUDA(cudaMemsetAsync(pl->d_repicked, 0, sizeof(unsigned long long), st));
+    SEMB_TRY(launch_repick(pl->w, R, st));
+    ++launches;
+  }
+  if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
+  pl->stats.kernel_launches = launches;
+  return SEMB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int semb_plan_use_graph(semb_plan* pl, int32_t on) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  pl->use_graph = on != 0;
+  if (!pl->use_graph && pl->graph) {
+    cudaGraphExecDestroy(pl->graph);
+    pl->graph = nullptr;
+  }
+  return SEMB_OK;
+}
+
+int semb_plan_run(semb_plan* pl) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_run before semb_plan_upload");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  cudaStream_t st = pl->stream;
+  SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, sizeof(int), st));
+  if (pl->use_graph) {
+    if (!pl->graph) {
+      cudaGraph_t graph;
+      SEMB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue_run(pl, true);
+      cudaError_t e = cudaStreamEndCapture(st, &graph);
+      if (rc != SEMB_OK) return rc;
+      SEMB_CUDA(e);
+      e = cudaGraphInstantiate(&pl->graph, graph, 0);
+      cudaGraphDestroy(graph);
+      SEMB_CUDA(e);
+    }
+    SEMB_CUDA(cudaGraphLaunch(pl->graph, st));
+  } else {
+    SEMB_TRY(enqueue_run(pl, true));
+  }
+  SEMB_CUDA(cudaStreamSynchronize(st));
+  int status = 0;
+  unsigned long long rep = 0;
+  SEMB_CUDA(cudaMemcpy(&status, pl->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (pl->p.mode == SEMB_BATCHED)
+    SEMB_CUDA(cudaMemcpy(&rep, pl->d_repicked, sizeof(rep), cudaMemcpyDeviceToHost));
+  float a = 0.f, b = 0.f, c = 0.f;
+  cudaEventElapsedTime(&a, pl->ev[1], pl->ev[2]);
+  cudaEventElapsedTime(&b, pl->ev[2], pl->ev[3]);
+  cudaEventElapsedTime(&c, pl->ev[0], pl->ev[3]);
+  pl->stats.ms_search = a;
+  pl->stats.ms_repick = b;
+  pl->stats.ms_total = c;
+  pl->stats.repicked = (int64_t)rep;
+  if (status & ST_TIMEOUT) return fail(SEMB_E_TIMEOUT, "a staging wait in the search kernel timed out");
+  if (status) return fail(SEMB_E_CUDA, "search kernel reported status %d", status);
+  return SEMB_OK;
+}
+
+int semb_plan_download(semb_plan* pl, int32_t* ctr, float* str, float* stk) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_download before semb_plan_upload");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  const size_t n = (size_t)pl->ncdps * pl->ns;
+  cudaStream_t st = pl->stream;
+  if (ctr) SEMB_CUDA(cudaMemcpyAsync(ctr, pl->d_ctr, n * 4, cudaMemcpyDeviceToHost, st));
+  if (str) SEMB_CUDA(cudaMemcpyAsync(str, pl->d_str, n * 4, cudaMemcpyDeviceToHost, st));
+  if (stk) SEMB_CUDA(cudaMemcpyAsync(stk, pl->d_stk, n * 4, cudaMemcpyDeviceToHost, st));
+  SEMB_CUDA(cudaStreamSynchronize(st));
+  return SEMB_OK;
+}
+
+int semb_plan_neighbours(semb_plan* pl, int32_t* off, int32_t* list, int64_t* n_out) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_neighbours before semb_plan_upload");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  if (n_out) *n_out = pl->n_nbr;
+  if (off) {
+    std::vector<int64_t> o(pl->ncdps + 1);
+    SEMB_CUDA(cudaMemcpy(o.data(), pl->d_nbr_off, o.size() * 8, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < o.size(); ++i) off[i] = (int32_t)o[i];
+  }
+  if (list) SEMB_CUDA(cudaMemcpy(list, pl->d_nbr, (size_t)pl->n_nbr * 4, cudaMemcpyDeviceToHost));
+  return SEMB_OK;
+}
+
+int semb_plan_stats(const semb_plan* pl, semb_stats* out) {
+  if (!pl || !out) return fail(SEMB_E_ARG, "null argument");
+  *out = pl->stats;
+  return SEMB_OK;
+}
+
+}  // extern "C"

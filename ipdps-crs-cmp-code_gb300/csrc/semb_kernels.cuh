@@ -1,0 +1,669 @@
+// Fused CMP/CRS semblance search kernels for sm_103a.
+//
+// One CTA works on one task: a CDP and a block of 32 consecutive output samples t0
+// (lane l of every warp owns t0 = t0_start + l).  The CTA walks the candidate grid
+// in passes; in a pass, warp w owns RC candidates, so each thread carries RC
+// (t0, candidate) items whose partial sums live in registers.  The CDP's aperture
+// traces are streamed through shared memory in chunks: warp 0 works out, for every
+// trace of the next chunk, the sample window that any item of this pass can touch
+// (from the pass's parameter bounds and the task's t0 range) and stages exactly
+// those windows, so every staged sample is reused by all items of the pass.
+// Semblance, stack and the per-t0 argmax are fused: the pick is reduced in
+// registers and then across warps through shared memory, and only ctr/str/stk (or,
+// in the fast form, the per-t0 top-4 list) leave the SM.
+//
+// Reference semantics (per item (t0, candidate), CMP/OpenMP/src/main.cpp:149-204,
+// CRS/OpenMP/src/main.cpp:209-267):
+//   CMP  t = sqrt((dt*t0)^2 + c*h) * idt
+//   CRS  t = (dt*t0 + a*|dm|)^2 + b*dm^2 + c*h;  t = t < 0 ? -1 : sqrt(t);  t *= idt
+//   it = (int)t, x = t - it; the trace is in range iff it-tau >= 0 && it+tau+1 < ns;
+//   for j < w: v = (s[it-tau+j+1] - s[it-tau+j]) * x + s[it-tau+j],
+//   num_j += v, den += v^2, lin += v, M++; out of range: err++.
+//   valid iff den > 1e-13 && M > 0 && err < 2: sem = sum_j num_j^2 / (den*M),
+//   stk = lin / (w*M); invalid: sem = stk = -1 (CMP) or 0 (CRS).
+//   Argmax per t0 (CMP main.cpp:207-222, CRS main.cpp:270-285): the first
+//   candidate (lowest index) with the largest semblance, which must exceed 0.
+//
+// Two forms share the structure:
+//   PLAIN  FP32 with the reference's operation order: every multiply and add is
+//          rounded separately (__fmul_rn/__fadd_rn: no contraction), IEEE sqrt
+//          and division, the same `lin` accumulator; bit-compatible with the
+//          reference's single-precision build.
+//   FAST   FP32 with fused multiply-adds, hardware sqrt, traveltimes in sample
+//          units (candidates pre-scaled by idt), the stack taken from sum_j num_j,
+//          and the energy sum accumulated per chunk and folded into a Kahan-
+//          compensated total; keeps the top-4 candidates per t0 for the FP64
+//          re-pick.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace semb {
+
+enum { METHOD_CMP = 0, METHOD_CRS = 1 };
+enum { FORM_PLAIN = 0, FORM_FAST = 1 };
+enum { STORE_F32 = 0, STORE_F16 = 1, STORE_BF16 = 2 };
+
+constexpr int kTB = 32;          // t0 samples per task (one per lane)
+constexpr int kMaxChunk = 128;   // aperture traces staged per chunk
+constexpr int kMargin = 2;       // extra samples on each side of a staged window
+constexpr int kTopK = 4;
+constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier wait (2 s), then error
+
+// Shared memory layout of the search kernel: barrier + control words, chunk
+// metadata, copy descriptors, then the staging buffer of `cap` floats.
+constexpr int kSmemHeader = 64;
+
+// Device status word bits.
+enum { ST_TIMEOUT = 1, ST_BAD_ARG = 2 };
+
+struct KParams {
+  // trace store, [ntr][pitch] (pitch a multiple of 8 elements)
+  const float* samples;         // FP32
+  const uint16_t* samples16;    // FP16 or BF16 bit patterns (fast form)
+  const float* scale;           // per-trace scale of samples16
+  int64_t pitch;
+  int storage;                  // STORE_*
+  // aperture lists: entries ap_off[c] .. ap_off[c+1]-1 of CDP c
+  const int64_t* ap_off;
+  const int32_t* ap_tr;         // trace index of each entry
+  const float4* ap_geo;         // (|dm|, dm^2, h, 0) per entry, FP32
+  // candidates in search order, padded to npass*cpp; .w holds the grid index bits
+  const float4* cand;
+  const float* pass_bounds;     // [npass][8]: amin amax bmin bmax cmin cmax (raw units)
+  int npass;
+  int cpp;                      // candidates per pass = warps * RC
+  // tasks (cdp, t0_start)
+  const int2* tasks;
+  int ntasks;
+  int* counter;                 // work-queue head (fast form)
+  // sampling
+  int ns;
+  int tau;
+  float dt, idt;
+  int cap;                      // staging buffer capacity (floats)
+  // outputs [ncdps][ns]
+  int32_t* ctr;
+  float* str;
+  float* stk;
+  const float* stt00;           // CRS: stack of item (t0=0, candidate 0) per CDP
+  float* top_sem;               // fast form: [ncdps][ns][4]
+  int32_t* top_idx;
+  float* top_stk;
+  int* status;
+};
+
+// ---------------------------------------------------------------------------
+// small PTX helpers (mbarrier + bulk copy)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// 1-D bulk copy global -> shared (TMA), completion counted on `bar` in bytes.
+// dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ float sqrt_fast(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float half_bits_to_float(uint32_t b) {
+  return __half2float(__ushort_as_half(static_cast<unsigned short>(b)));
+}
+
+// Pick order: larger semblance first; equal semblance -> lower grid index first.
+__device__ __forceinline__ bool better(float s, int i, float bs, int bi) {
+  return s > bs || (s == bs && i < bi);
+}
+
+// ---------------------------------------------------------------------------
+// staging plan: warp 0 sizes and stages the next chunk of aperture entries.
+
+struct ChunkMeta {
+  float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
+  int n;                   // entries in this chunk
+  int bytes;               // bytes staged (TMA form)
+};
+
+// Sample window [lo, hi] of one trace that items of a pass can read, for t0 in
+// [T_lo, T_hi] (seconds) and parameters within the pass bounds.  Returns false
+// when no item can be in range.
+template <int METHOD>
+__device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_lo, float T_hi, float idt,
+                                             int tau, int ns, int& lo, int& hi) {
+  float t2min, t2max;
+  if (METHOD == METHOD_CMP) {
+    // t^2 = t0^2 + c*h, h >= 0
+    t2min = T_lo * T_lo + fminf(pb[4] * g.z, pb[5] * g.z);
+    t2max = T_hi * T_hi + fmaxf(pb[4] * g.z, pb[5] * g.z);
+  } else {
+    // t^2 = (t0 + a*m)^2 + b*m2 + c*h with m, m2, h >= 0
+    float ulo = T_lo + pb[0] * g.x, uhi = T_hi + pb[1] * g.x;
+    float u2lo = (ulo <= 0.f && uhi >= 0.f) ? 0.f : fminf(ulo * ulo, uhi * uhi);
+    float u2hi = fmaxf(ulo * ulo, uhi * uhi);
+    t2min = u2lo + pb[2] * g.y + pb[4] * g.z;
+    t2max = u2hi + pb[3] * g.y + pb[5] * g.z;
+  }
+  // relative slack for rounding differences between this bound and the items
+  t2min -= fabsf(t2min) * 1e-5f;
+  t2max += fabsf(t2max) * 1e-5f;
+  if (!(t2max >= 0.f)) {
+    // every item has a negative t^2 (or the bound is not finite): nothing in range
+    if (t2max < 0.f) return false;
+    lo = 0;
+    hi = ns - 1;
+    return true;
+  }
+  float smin = t2min > 0.f ? sqrtf(t2min) * idt : 0.f;
+  float smax = sqrtf(t2max) * idt;
+  smin = fminf(smin, (float)ns + 8.f);
+  smax = fminf(smax, (float)ns + 8.f);
+  lo = (int)smin - tau - kMargin;
+  hi = (int)smax + tau + 1 + kMargin;
+  lo = max(lo, 0);
+  hi = min(hi, ns - 1);
+  return lo <= hi;
+}
+
+// Warp 0: choose the entries of the next chunk starting at ap_pos and record, per
+// entry, its geometry, its shared-memory offset and its source window (trace,
+// first sample, length, offset) in `src`.  ALIGN is the window alignment in
+// samples: 4 for FP32 bulk copies (16 bytes), 8 for 16-bit sources.
+template <int METHOD, int FORM>
+__device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, int64_t ap_end, float T_lo,
+                           float T_hi, ChunkMeta* meta, int4* src) {
+  const int lane = threadIdx.x & 31;
+  constexpr int ALIGN = (FORM == FORM_PLAIN) ? 4 : 8;
+  int base = 0;   // floats used in the staging buffer
+  int n = 0;
+  for (int round = 0; round < kMaxChunk / 32; ++round) {
+    int64_t k = ap_pos + n + lane;
+    bool have = k < ap_end;
+    float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+    int lo = 0, hi = -1;
+    int len = 0;
+    if (have) {
+      g = P.ap_geo[k];
+      if (trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi)) {
+        lo &= ~(ALIGN - 1);
+        hi |= (ALIGN - 1);
+        len = hi - lo + 1;
+      }
+    }
+    // inclusive scan of the window lengths over the warp
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const bool fits = have && (base + incl <= P.cap);
+    const int nfit = __popc(__ballot_sync(0xffffffffu, fits));   // fits holds for a prefix of lanes
+    if (fits) {
+      const int off = base + incl - len;
+      g.w = __int_as_float(off - lo);
+      meta->geo[n + lane] = g;
+      src[n + lane] = make_int4(P.ap_tr[k], lo, len, off);
+    }
+    base += nfit > 0 ? __shfl_sync(0xffffffffu, incl, nfit - 1) : 0;
+    n += nfit;
+    if (nfit < 32) break;
+  }
+  if (lane == 0) {
+    meta->n = n;
+    meta->bytes = base * 4;
+  }
+}
+
+// Warp 0, after plan_chunk (FP32 store): announce the chunk's bytes on the
+// barrier, then start one bulk copy per staged window.
+__device__ __forceinline__ void issue_chunk_copies(const KParams& P, ChunkMeta* meta, const int4* src, float* buf,
+                                                   uint64_t* bar) {
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)meta->bytes);
+  __syncwarp();
+  const int n = meta->n;
+  for (int e = lane; e < n; e += 32) {
+    const int4 si = src[e];
+    if (si.z > 0) bulk_g2s(buf + si.w, P.samples + (int64_t)si.x * P.pitch + si.y, (uint32_t)si.z * 4u, bar);
+  }
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// item arithmetic
+
+template <int W>
+struct PlainAcc {
+  float num[W];
+  float den, lin;
+  int M;
+};
+
+template <int W>
+struct FastAcc {
+  float num[W];
+  float den_c;      // energy of the current chunk
+  float den_hi;     // Kahan-compensated total
+  float den_lo;     // compensation
+  int M;
+};
+
+// ---------------------------------------------------------------------------
+// The search kernel.
+
+template <int METHOD, int FORM, int W, int RC>
+__global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  int* ctl = reinterpret_cast<int*>(smem_raw + 16);
+  ChunkMeta* meta = reinterpret_cast<ChunkMeta*>(smem_raw + 64);
+  int4* srcinfo = reinterpret_cast<int4*>(smem_raw + 64 + ((sizeof(ChunkMeta) + 127) / 128) * 128);
+  float* buf = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(srcinfo) + kMaxChunk * sizeof(int4));
+
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  constexpr float kSent = (METHOD == METHOD_CMP) ? -1.0f : 0.0f;
+
+  if (threadIdx.x == 0 && FORM == FORM_PLAIN) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+
+  int task_iter = 0;
+  for (;;) {
+    int task;
+    if (FORM == FORM_PLAIN) {
+      if (task_iter > 0) break;
+      task = blockIdx.x;
+    } else {
+      if (threadIdx.x == 0) ctl[0] = atomicAdd(P.counter, 1);
+      __syncthreads();
+      task = ctl[0];
+      __syncthreads();
+    }
+    ++task_iter;
+    if (task >= P.ntasks) break;
+
+    const int2 td = P.tasks[task];
+    const int cdp = td.x;
+    const int t0s = td.y;
+    const int t0 = min(t0s + lane, P.ns - 1);
+    const int t0hi = min(t0s + kTB - 1, P.ns - 1);
+    const int64_t ap_begin = P.ap_off[cdp];
+    const int64_t ap_end = P.ap_off[cdp + 1];
+    const int napert = (int)(ap_end - ap_begin);
+    const float T_lo = P.dt * (float)t0s;
+    const float T_hi = P.dt * (float)t0hi;
+
+    // per-thread running pick for this lane's t0
+    float best_s[FORM == FORM_FAST ? kTopK : 1];
+    int best_i[FORM == FORM_FAST ? kTopK : 1];
+    float best_k[FORM == FORM_FAST ? kTopK : 1];
+#pragma unroll
+    for (int q = 0; q < (FORM == FORM_FAST ? kTopK : 1); ++q) {
+      best_s[q] = 0.f;
+      best_i[q] = 0x7fffffff;
+      best_k[q] = 0.f;
+    }
+
+    // per-lane time values
+    const float Tsec = __fmul_rn(P.dt, (float)t0);            // reference: _t0 = dt * t0
+    const float T2sec = __fmul_rn(Tsec, Tsec);                 // CMP: _t0 * _t0
+    const float Tsmp = (float)t0;                              // fast form: sample units
+    const float T2smp = Tsmp * Tsmp;
+    const float tau_lo = (float)P.tau;
+    const float tau_hi = (float)(P.ns - P.tau - 1);
+
+    for (int pass = 0; pass < P.npass; ++pass) {
+      const float* pb = P.pass_bounds + pass * 8;
+      float ca[RC], cb[RC], cc[RC];
+      int ci[RC];
+#pragma unroll
+      for (int r = 0; r < RC; ++r) {
+        float4 cv = P.cand[pass * P.cpp + warp * RC + r];
+        ca[r] = cv.x;
+        cb[r] = cv.y;
+        cc[r] = cv.z;
+        ci[r] = __float_as_int(cv.w);
+      }
+      PlainAcc<W> pa[FORM == FORM_PLAIN ? RC : 1];
+      FastAcc<W> fa[FORM == FORM_FAST ? RC : 1];
+      if (FORM == FORM_PLAIN) {
+#pragma unroll
+        for (int r = 0; r < RC; ++r) {
+#pragma unroll
+          for (int j = 0; j < W; ++j) pa[r].num[j] = 0.f;
+          pa[r].den = 0.f;
+          pa[r].lin = 0.f;
+          pa[r].M = 0;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < RC; ++r) {
+#pragma unroll
+          for (int j = 0; j < W; ++j) fa[r].num[j] = 0.f;
+          fa[r].den_c = 0.f;
+          fa[r].den_hi = 0.f;
+          fa[r].den_lo = 0.f;
+          fa[r].M = 0;
+        }
+      }
+
+      int64_t ap_pos = ap_begin;
+      while (ap_pos < ap_end) {
+        if (warp == 0) {
+          plan_chunk<METHOD, FORM>(P, pb, ap_pos, ap_end, T_lo, T_hi, meta, srcinfo);
+          if (FORM == FORM_PLAIN) issue_chunk_copies(P, meta, srcinfo, buf, bar);
+        }
+        __syncthreads();
+        const int n = meta->n;
+        if (FORM == FORM_PLAIN) {
+          // wait for the bulk copies of this chunk; give up after kWaitNs
+          bool ok = true;
+          if (!mbar_try_wait(bar, phase)) {
+            const uint64_t t_start = global_ns();
+            while (!mbar_try_wait(bar, phase)) {
+              if (global_ns() - t_start > kWaitNs) {
+                ok = false;
+                break;
+              }
+            }
+          }
+          phase ^= 1u;
+          if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicOr(P.status, ST_TIMEOUT);
+            return;
+          }
+        } else {
+          // cooperative copy: 16-bit or FP32 store -> FP32 x scale in shared memory
+          for (int e = warp; e < n; e += nwarps) {
+            int4 si = srcinfo[e];   // (trace, lo, len, off)
+            if (si.z <= 0) continue;
+            float* dst = buf + si.w;
+            if (P.storage == STORE_F32) {
+              const float4* src = reinterpret_cast<const float4*>(P.samples + (int64_t)si.x * P.pitch + si.y);
+              for (int q = lane; q < (si.z >> 2); q += 32) reinterpret_cast<float4*>(dst)[q] = __ldg(src + q);
+            } else {
+              const float sc = __ldg(P.scale + si.x);
+              const uint4* src = reinterpret_cast<const uint4*>(P.samples16 + (int64_t)si.x * P.pitch + si.y);
+              for (int q = lane; q < (si.z >> 3); q += 32) {
+                uint4 v = __ldg(src + q);
+                uint32_t wv[4] = {v.x, v.y, v.z, v.w};
+                float o[8];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                  if (P.storage == STORE_F16) {
+                    o[2 * u] = half_bits_to_float(wv[u] & 0xffffu) * sc;
+                    o[2 * u + 1] = half_bits_to_float(wv[u] >> 16) * sc;
+                  } else {
+                    o[2 * u] = __uint_as_float(wv[u] << 16) * sc;
+                    o[2 * u + 1] = __uint_as_float(wv[u] & 0xffff0000u) * sc;
+                  }
+                }
+                reinterpret_cast<float4*>(dst)[2 * q] = make_float4(o[0], o[1], o[2], o[3]);
+                reinterpret_cast<float4*>(dst)[2 * q + 1] = make_float4(o[4], o[5], o[6], o[7]);
+              }
+            }
+          }
+          __syncthreads();
+        }
+
+        const unsigned clamp_hi = (unsigned)(P.cap - W - 1);
+        for (int e = 0; e < n; ++e) {
+          const float4 g = meta->geo[e];
+          const int soff = __float_as_int(g.w);
+          if (FORM == FORM_PLAIN) {
+#pragma unroll
+            for (int r = 0; r < RC; ++r) {
+              float t;
+              if (METHOD == METHOD_CMP) {
+                t = __fmul_rn(__fsqrt_rn(__fadd_rn(T2sec, __fmul_rn(cc[r], g.z))), P.idt);
+              } else {
+                t = __fadd_rn(Tsec, __fmul_rn(ca[r], g.x));
+                t = __fadd_rn(__fadd_rn(__fmul_rn(t, t), __fmul_rn(cb[r], g.y)), __fmul_rn(cc[r], g.z));
+                t = (t < 0.0f) ? -1.0f : __fsqrt_rn(t);
+                t = __fmul_rn(t, P.idt);
+              }
+              if (t >= tau_lo && t < tau_hi) {
+                const float y = __fadd_rz(t, 8388608.0f);
+                const int it = __float_as_int(y) - 0x4B000000;
+                const float x = __fsub_rn(t, __fsub_rn(y, 8388608.0f));
+                unsigned idx = (unsigned)(soff + it - P.tau);
+                idx = min(idx, clamp_hi);
+                const float* s = buf + idx;
+                float s1 = s[0];
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                  const float s0 = s1;
+                  s1 = s[j + 1];
+                  const float v = __fadd_rn(__fmul_rn(__fsub_rn(s1, s0), x), s0);
+                  pa[r].num[j] = __fadd_rn(pa[r].num[j], v);
+                  pa[r].den = __fadd_rn(pa[r].den, __fmul_rn(v, v));
+                  pa[r].lin = __fadd_rn(pa[r].lin, v);
+                }
+                pa[r].M += 1;
+              }
+            }
+          } else {
+            const unsigned span = (unsigned)(P.ns - 2 * P.tau - 2);
+#pragma unroll
+            for (int r = 0; r < RC; ++r) {
+              float t2;
+              if (METHOD == METHOD_CMP) {
+                t2 = fmaf(cc[r], g.z, T2smp);
+              } else {
+                const float u = fmaf(ca[r], g.x, Tsmp);
+                t2 = fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
+              }
+              const float t = sqrt_fast(t2);
+              const float y = __fadd_rz(t, 8388608.0f);
+              const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
+              if ((unsigned)rel <= span) {
+                const float x = t - (y - 8388608.0f);
+                unsigned idx = min((unsigned)(soff + rel), clamp_hi);
+                const float* s = buf + idx;
+                float s1 = s[0];
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                  const float s0 = s1;
+                  s1 = s[j + 1];
+                  const float v = fmaf(s1 - s0, x, s0);
+                  fa[r].num[j] += v;
+                  fa[r].den_c = fmaf(v, v, fa[r].den_c);
+                }
+                fa[r].M += 1;
+              }
+            }
+          }
+        }
+        if (FORM == FORM_FAST) {
+#pragma unroll
+          for (int r = 0; r < RC; ++r) {
+            // Kahan: fold this chunk's energy into the compensated total
+            const float yv = fa[r].den_c - fa[r].den_lo;
+            const float tv = fa[r].den_hi + yv;
+            fa[r].den_lo = (tv - fa[r].den_hi) - yv;
+            fa[r].den_hi = tv;
+            fa[r].den_c = 0.f;
+          }
+        }
+        ap_pos += n;
+        __syncthreads();   // buffer and meta free for the next chunk
+      }
+
+      // finalize the pass's items and fold them into this lane's pick
+#pragma unroll
+      for (int r = 0; r < RC; ++r) {
+        float sem, stk;
+        if (FORM == FORM_PLAIN) {
+          float acsq = 0.f;
+#pragma unroll
+          for (int j = 0; j < W; ++j) acsq = __fadd_rn(acsq, __fmul_rn(pa[r].num[j], pa[r].num[j]));
+          const float mf = (float)pa[r].M;
+          const int err = napert - pa[r].M;
+          const bool ok = ((double)pa[r].den > 1e-13) && ((double)mf > 1e-13) && (err < 2);
+          sem = ok ? __fdiv_rn(acsq, __fmul_rn(pa[r].den, mf)) : kSent;
+          stk = ok ? __fdiv_rn(pa[r].lin, __fmul_rn((float)W, mf)) : kSent;
+        } else {
+          float acsq = 0.f, lin = 0.f;
+#pragma unroll
+          for (int j = 0; j < W; ++j) {
+            acsq = fmaf(fa[r].num[j], fa[r].num[j], acsq);
+            lin += fa[r].num[j];
+          }
+          const float den = fa[r].den_hi - fa[r].den_lo;
+          const float mf = (float)fa[r].M;
+          const int err = napert - fa[r].M;
+          const bool ok = ((double)den > 1e-13) && (fa[r].M > 0) && (err < 2);
+          sem = ok ? __fdividef(acsq, den * mf) : kSent;
+          stk = ok ? __fdividef(lin, (float)W * mf) : kSent;
+        }
+        const int idx = ci[r];
+        if (FORM == FORM_PLAIN) {
+          if (sem > 0.f && better(sem, idx, best_s[0], best_i[0])) {
+            best_s[0] = sem;
+            best_i[0] = idx;
+            best_k[0] = stk;
+          }
+        } else {
+          // sorted insert into the top-4 (descending semblance, ascending index)
+          if (sem > 0.f && better(sem, idx, best_s[kTopK - 1], best_i[kTopK - 1])) {
+            float cs = sem, ck = stk;
+            int cidx = idx;
+#pragma unroll
+            for (int q = 0; q < kTopK; ++q) {
+              if (better(cs, cidx, best_s[q], best_i[q])) {
+                const float ts = best_s[q], tk = best_k[q];
+                const int ti = best_i[q];
+                best_s[q] = cs;
+                best_i[q] = cidx;
+                best_k[q] = ck;
+                cs = ts;
+                cidx = ti;
+                ck = tk;
+              }
+            }
+          }
+        }
+      }
+    }
+
+    // reduce the picks of all warps for each t0 (lane) through shared memory
+    __syncthreads();
+    constexpr int K = (FORM == FORM_FAST) ? kTopK : 1;
+    float* rs = buf;                                   // [nwarps][32][K]
+    int* ri = reinterpret_cast<int*>(buf + nwarps * 32 * K);
+    float* rk = buf + 2 * nwarps * 32 * K;
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      rs[(warp * 32 + lane) * K + q] = best_s[q];
+      ri[(warp * 32 + lane) * K + q] = best_i[q];
+      rk[(warp * 32 + lane) * K + q] = best_k[q];
+    }
+    __syncthreads();
+    if (warp == 0) {
+      float fs[K], fk[K];
+      int fi[K];
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        fs[q] = 0.f;
+        fi[q] = 0x7fffffff;
+        fk[q] = 0.f;
+      }
+      for (int w2 = 0; w2 < nwarps; ++w2) {
+        for (int q2 = 0; q2 < K; ++q2) {
+          float cs = rs[(w2 * 32 + lane) * K + q2];
+          int cidx = ri[(w2 * 32 + lane) * K + q2];
+          float ck = rk[(w2 * 32 + lane) * K + q2];
+          if (!(cs > 0.f)) continue;
+#pragma unroll
+          for (int q = 0; q < K; ++q) {
+            if (better(cs, cidx, fs[q], fi[q])) {
+              const float ts = fs[q], tk = fk[q];
+              const int ti = fi[q];
+              fs[q] = cs;
+              fi[q] = cidx;
+              fk[q] = ck;
+              cs = ts;
+              cidx = ti;
+              ck = tk;
+            }
+          }
+        }
+      }
+      const int tt = t0s + lane;
+      if (tt < P.ns) {
+        const int64_t o = (int64_t)cdp * P.ns + tt;
+        if (FORM == FORM_PLAIN) {
+          if (fs[0] > 0.f) {
+            P.ctr[o] = fi[0];
+            P.str[o] = fs[0];
+            P.stk[o] = fk[0];
+          } else {
+            // no candidate above 0: CMP ctr -1, stack 0 (CMP main.cpp:219-221);
+            // CRS ctr 0 and the stack of item (t0 = 0, candidate 0) (CRS main.cpp:282-284)
+            P.ctr[o] = (METHOD == METHOD_CMP) ? -1 : 0;
+            P.str[o] = 0.f;
+            P.stk[o] = (METHOD == METHOD_CMP) ? 0.f : P.stt00[cdp];
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < K; ++q) {
+            P.top_sem[o * kTopK + q] = fs[q];
+            P.top_idx[o * kTopK + q] = fs[q] > 0.f ? fi[q] : -1;
+            P.top_stk[o * kTopK + q] = fk[q];
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace semb

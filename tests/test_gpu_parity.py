@@ -1,0 +1,75 @@
+"""CUDA path vs the oracle, through the C ABI (GPU)."""
+import numpy as np
+import pytest
+
+import oracle
+import semb
+import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _arrays(g):
+    return semb.GatherArrays(g["ntraces_by_cdp_id"], g["ns"], g["dt_us"], g["gx"], g["gy"], g["sx"], g["sy"],
+                             g["scalco"], g["samples"])
+
+
+def _run(method, g, params, **kw):
+    with semb.Plan(semb.params(method, **params, **kw)) as p:
+        p.upload(_arrays(g).view())
+        p.run()
+        out = p.download()
+        st = p.stats()
+    return out, st
+
+
+@pytest.mark.parametrize("ns,fold,nc,tau", [(400, 24, 33, 0.002), (500, 30, 101, 0.004), (300, 7, 16, 0.0)])
+def test_cmp_plain_matches_oracle_f32(ns, fold, nc, tau):
+    s = synth.cmp_survey(seed=21, ncmp=10, fold=fold, ns=ns, nc=nc, tau=tau)
+    g = oracle.gather(s.headers, s.samples, "cmp", s.params["aph"])
+    ref = oracle.cmp(g, s.params, "f32")
+    (ctr, sem, stk), _ = _run(semb.CMP, g, s.params, mode=semb.PLAIN_F32)
+    assert np.array_equal(ctr, ref["ctr"])
+    np.testing.assert_allclose(sem, ref["str"], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(stk, ref["stk"], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("na,nb,nc,tau", [(5, 5, 5, 0.002), (3, 4, 7, 0.004), (2, 1, 3, 0.0)])
+def test_crs_plain_matches_oracle_f32(na, nb, nc, tau):
+    s = synth.crs_survey(seed=22, ncdp=12, noffsets=16, ns=300, na=na, nb=nb, nc=nc, tau=tau)
+    g = oracle.gather(s.headers, s.samples, "crs", s.params["aph"], s.params["apm"], real=np.float32)
+    ref = oracle.crs(g, s.params, "f32")
+    (ctr, sem, stk), _ = _run(semb.CRS, g, s.params, mode=semb.PLAIN_F32)
+    assert np.array_equal(ctr, ref["ctr"])
+    np.testing.assert_allclose(sem, ref["str"], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(stk, ref["stk"], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("storage", [semb.STORE_F16, semb.STORE_BF16, semb.STORE_F32])
+def test_crs_batched_close_to_oracle_f64(storage):
+    s = synth.crs_survey(seed=23, ncdp=12, noffsets=16, ns=300, na=5, nb=5, nc=5)
+    g = oracle.gather(s.headers, s.samples, "crs", s.params["aph"], s.params["apm"], real=np.float64)
+    ref = oracle.crs(g, s.params, "f64")
+    (ctr, sem, stk), st = _run(semb.CRS, g, s.params, mode=semb.BATCHED, storage=storage)
+    tol = 5e-3 if storage == semb.STORE_BF16 else 1e-3
+    assert np.max(np.abs(sem - ref["str"])) < tol
+    assert np.mean(ctr == ref["ctr"]) > 0.99
+
+
+def test_cmp_batched_close_to_oracle_f64():
+    s = synth.cmp_survey(seed=24, ncmp=10, fold=24, ns=400, nc=33)
+    g = oracle.gather(s.headers, s.samples, "cmp", s.params["aph"], real=np.float64)
+    ref = oracle.cmp(g, s.params, "f64")
+    (ctr, sem, stk), st = _run(semb.CMP, g, s.params, mode=semb.BATCHED)
+    assert np.max(np.abs(sem - ref["str"])) < 1e-3
+    assert np.mean(ctr == ref["ctr"]) > 0.99
+
+
+def test_crs_neighbour_lists_match_reference_rule():
+    s = synth.crs_survey(seed=25, ncdp=30, noffsets=6, ns=200, na=2, nb=2, nc=2)
+    g = oracle.gather(s.headers, s.samples, "crs", s.params["aph"], s.params["apm"], real=np.float32)
+    with semb.Plan(semb.params(semb.CRS, **s.params)) as p:
+        p.upload(_arrays(g).view())
+        off, lst = p.neighbours()
+    assert np.array_equal(off, g["nbr_off"])
+    assert np.array_equal(lst, g["nbr"])
