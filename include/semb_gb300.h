@@ -177,8 +177,10 @@ int semb_plan_download(semb_plan* plan, int32_t* ctr, float* str, float* stk);
 int semb_plan_neighbours(semb_plan* plan, int32_t* off, int32_t* list, int64_t* n_out);
 
 typedef struct semb_stats {
-  double ms_search;       /* device time of the last run's semblance kernel(s) */
-  double ms_repick;       /* device time of the last run's FP64 re-pick kernel */
+  double ms_search;       /* device time of the last run's semblance kernel(s);
+                             0 when the run was a graph replay */
+  double ms_repick;       /* device time of the last run's FP64 re-pick kernel;
+                             0 when the run was a graph replay */
   double ms_total;        /* device time of the whole last run */
   double ms_upload;       /* device time of the last upload (copies + binning) */
   int64_t evals;          /* (CDP, t0, candidate) semblance evaluations per run */
@@ -206,6 +208,11 @@ int semb_plan_destroy(semb_plan* plan);
 /* Page-locked host memory for input/output buffers (cudaMallocHost). */
 int semb_host_alloc(size_t bytes, void** out);
 int semb_host_free(void* p);
+
+/* Diagnostic with no counterpart in the reference: measured FP32 fused-multiply-
+ * add throughput of `device` in TFLOP/s (2 flops per FMA), the denominator of the
+ * search kernels' roofline, which are bound by FP32 issue rather than HBM. */
+int semb_probe_fp32(int32_t device, double* tflops);
 
 /* Number of visible CUDA devices (0 when none); never fails. */
 int32_t semb_device_count(void);

@@ -320,7 +320,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   pl->ns = g->ns;
   pl->dt_us = g->dt_us;
   pl->ntraces = g->ntraces;
-  pl->pitch = (g->ns + 7) & ~7;
+  pl->pitch = ((g->ns + 7) & ~7) + 8;   // >= 8 zero samples after each trace
 
   // time sampling (CMP/OpenMP/src/main.cpp:107-110, CRS/OpenMP/src/main.cpp:135-138)
   {
@@ -542,13 +542,15 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
     SEMB_TRY(dev_alloc(&pl->d_top_stk, nout * kTopK));
   }
 
-  // staging capacity: as large as two resident CTAs per SM allow, at least one trace
+  // staging capacity: as large as two resident CTAs per SM allow (about 113 KB of
+  // shared memory each), and never less than one whole trace
   const size_t fixed = 64 + ((sizeof(ChunkMeta) + 127) / 128) * 128 + kMaxChunk * sizeof(int4);
-  int cap = 24576;
-  cap = std::max<int>(cap, (int)pl->pitch + 16);
-  cap = (cap + 7) & ~7;
+  const size_t unit = form == FORM_PLAIN ? sizeof(float) : sizeof(float4);
+  const size_t budget = 113 * 1024 - fixed - kZeroSlots * unit;
+  int cap = (int)(budget / unit) & ~7;
+  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 7) & ~7;
   pl->cap = cap;
-  pl->smem = fixed + (size_t)cap * sizeof(float);
+  pl->smem = fixed + ((size_t)cap + kZeroSlots) * unit;
   if (pl->smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", g->ns);
   SEMB_TRY(search_occupancy(p.method, form, pl->w, pl->nwarps, pl->smem, &pl->ctas_per_sm));
   if (pl->ctas_per_sm <= 0) return fail(SEMB_E_CUDA, "search kernel cannot be resident with %zu bytes", pl->smem);
@@ -699,7 +701,7 @@ int semb_plan_run(semb_plan* pl) {
     if (!pl->graph) {
       cudaGraph_t graph;
       SEMB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      int rc = enqueue_run(pl, true);
+      int rc = enqueue_run(pl, false);
       cudaError_t e = cudaStreamEndCapture(st, &graph);
       if (rc != SEMB_OK) return rc;
       SEMB_CUDA(e);
@@ -707,7 +709,9 @@ int semb_plan_run(semb_plan* pl) {
       cudaGraphDestroy(graph);
       SEMB_CUDA(e);
     }
+    SEMB_CUDA(cudaEventRecord(pl->ev[0], st));
     SEMB_CUDA(cudaGraphLaunch(pl->graph, st));
+    SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
   } else {
     SEMB_TRY(enqueue_run(pl, true));
   }
@@ -717,10 +721,13 @@ int semb_plan_run(semb_plan* pl) {
   SEMB_CUDA(cudaMemcpy(&status, pl->d_status, sizeof(int), cudaMemcpyDeviceToHost));
   if (pl->p.mode == SEMB_BATCHED)
     SEMB_CUDA(cudaMemcpy(&rep, pl->d_repicked, sizeof(rep), cudaMemcpyDeviceToHost));
+  // graph replays are timed as a whole; the per-kernel split needs direct launches
   float a = 0.f, b = 0.f, c = 0.f;
-  cudaEventElapsedTime(&a, pl->ev[1], pl->ev[2]);
-  cudaEventElapsedTime(&b, pl->ev[2], pl->ev[3]);
-  cudaEventElapsedTime(&c, pl->ev[0], pl->ev[3]);
+  if (!pl->use_graph) {
+    SEMB_CUDA(cudaEventElapsedTime(&a, pl->ev[1], pl->ev[2]));
+    SEMB_CUDA(cudaEventElapsedTime(&b, pl->ev[2], pl->ev[3]));
+  }
+  SEMB_CUDA(cudaEventElapsedTime(&c, pl->ev[0], pl->ev[3]));
   pl->stats.ms_search = a;
   pl->stats.ms_repick = b;
   pl->stats.ms_total = c;

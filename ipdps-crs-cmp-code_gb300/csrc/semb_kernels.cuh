@@ -24,16 +24,25 @@
 //   Argmax per t0 (CMP main.cpp:207-222, CRS main.cpp:270-285): the first
 //   candidate (lowest index) with the largest semblance, which must exceed 0.
 //
+// Items carry no branch: an out-of-range trace reads a block of zeros kept at the
+// end of the staging buffer with interpolation weight 0, so it adds exactly +0 to
+// the sums, and only M counts it out.  The RC items of a thread are then straight-
+// line code the compiler can interleave.
+//
 // Two forms share the structure:
 //   PLAIN  FP32 with the reference's operation order: every multiply and add is
 //          rounded separately (__fmul_rn/__fadd_rn: no contraction), IEEE sqrt
-//          and division, the same `lin` accumulator; bit-compatible with the
-//          reference's single-precision build.
-//   FAST   FP32 with fused multiply-adds, hardware sqrt, traveltimes in sample
-//          units (candidates pre-scaled by idt), the stack taken from sum_j num_j,
-//          and the energy sum accumulated per chunk and folded into a Kahan-
-//          compensated total; keeps the top-4 candidates per t0 for the FP64
-//          re-pick.
+//          and division, the same `lin` accumulator; staged by 1-D bulk copies
+//          (TMA) of the FP32 trace store.  Bit-compatible with the reference's
+//          single-precision build.
+//   FAST   traces stored as FP16/BF16 (+ FP32 scale) or FP32, staged as 16-byte
+//          entries (s_k, s_k+1 - s_k, s_k+1, s_k+2 - s_k+1) so that a w-sample
+//          window is ceil(w/2) vector loads and one FMA per interpolated sample;
+//          FP32 arithmetic with fused multiply-adds and hardware sqrt, traveltimes
+//          in sample units (candidates pre-scaled by idt), the stack taken from
+//          sum_j num_j, and the energy accumulated per chunk and folded into a
+//          Kahan-compensated total; keeps the top-4 candidates per t0 for the
+//          FP64 re-pick.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -50,17 +59,15 @@ constexpr int kTB = 32;          // t0 samples per task (one per lane)
 constexpr int kMaxChunk = 128;   // aperture traces staged per chunk
 constexpr int kMargin = 2;       // extra samples on each side of a staged window
 constexpr int kTopK = 4;
+constexpr int kZeroSlots = 16;   // zero block after the staging buffer (floats or entries)
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier wait (2 s), then error
-
-// Shared memory layout of the search kernel: barrier + control words, chunk
-// metadata, copy descriptors, then the staging buffer of `cap` floats.
-constexpr int kSmemHeader = 64;
 
 // Device status word bits.
 enum { ST_TIMEOUT = 1, ST_BAD_ARG = 2 };
 
 struct KParams {
-  // trace store, [ntr][pitch] (pitch a multiple of 8 elements)
+  // trace store, [ntr][pitch]; pitch is a multiple of 8 elements with at least 8
+  // zero elements after the last sample of each trace
   const float* samples;         // FP32
   const uint16_t* samples16;    // FP16 or BF16 bit patterns (fast form)
   const float* scale;           // per-trace scale of samples16
@@ -83,7 +90,7 @@ struct KParams {
   int ns;
   int tau;
   float dt, idt;
-  int cap;                      // staging buffer capacity (floats)
+  int cap;                      // staging capacity: floats (plain) or 16-byte entries (fast)
   // outputs [ncdps][ns]
   int32_t* ctr;
   float* str;
@@ -135,6 +142,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
           smem_u32(dst)),
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
 __device__ __forceinline__ float sqrt_fast(float x) {
@@ -202,15 +215,17 @@ __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_
 }
 
 // Warp 0: choose the entries of the next chunk starting at ap_pos and record, per
-// entry, its geometry, its shared-memory offset and its source window (trace,
-// first sample, length, offset) in `src`.  ALIGN is the window alignment in
-// samples: 4 for FP32 bulk copies (16 bytes), 8 for 16-bit sources.
+// entry, its geometry, its buffer offset (minus the window start, so that an item
+// indexes with it - tau directly) and its source window (trace, first sample,
+// length, offset) in `src`.  Windows are aligned to ALIGN samples: 4 for FP32 bulk
+// copies (16 bytes), 8 for the fast form's 8-sample staging groups.  Buffer units:
+// floats (plain) or one 16-byte entry per sample (fast).
 template <int METHOD, int FORM>
 __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, int64_t ap_end, float T_lo,
                            float T_hi, ChunkMeta* meta, int4* src) {
   const int lane = threadIdx.x & 31;
   constexpr int ALIGN = (FORM == FORM_PLAIN) ? 4 : 8;
-  int base = 0;   // floats used in the staging buffer
+  int base = 0;
   int n = 0;
   for (int round = 0; round < kMaxChunk / 32; ++round) {
     int64_t k = ap_pos + n + lane;
@@ -251,7 +266,7 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
   }
 }
 
-// Warp 0, after plan_chunk (FP32 store): announce the chunk's bytes on the
+// Warp 0, after plan_chunk (plain form): announce the chunk's bytes on the
 // barrier, then start one bulk copy per staged window.
 __device__ __forceinline__ void issue_chunk_copies(const KParams& P, ChunkMeta* meta, const int4* src, float* buf,
                                                    uint64_t* bar) {
@@ -266,14 +281,51 @@ __device__ __forceinline__ void issue_chunk_copies(const KParams& P, ChunkMeta* 
   }
 }
 
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
+// Fast form: all warps turn the chunk's windows into (s, ds) entries.  Each lane
+// handles 8 samples at a time (one 16-byte load of 16-bit samples, or two of FP32)
+// plus the 2 samples after them for the differences.
+__device__ __forceinline__ void stage_fast(const KParams& P, int n, const int4* src, float4* bufq) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int e = warp; e < n; e += nwarps) {
+    const int4 si = src[e];   // (trace, lo, len, off)
+    if (si.z <= 0) continue;
+    float4* dst = bufq + si.w;
+    const int groups = si.z >> 3;
+    float s[10];
+    for (int q = lane; q < groups; q += 32) {
+      if (P.storage == STORE_F32) {
+        const float* row = P.samples + (int64_t)si.x * P.pitch + si.y + 8 * q;
+        const float4 a = __ldg(reinterpret_cast<const float4*>(row));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(row) + 1);
+        const float2 c = __ldg(reinterpret_cast<const float2*>(row + 8));
+        s[0] = a.x; s[1] = a.y; s[2] = a.z; s[3] = a.w;
+        s[4] = b.x; s[5] = b.y; s[6] = b.z; s[7] = b.w;
+        s[8] = c.x; s[9] = c.y;
+      } else {
+        const float sc = __ldg(P.scale + si.x);
+        const uint16_t* row = P.samples16 + (int64_t)si.x * P.pitch + si.y + 8 * q;
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(row));
+        const uint32_t nx = __ldg(reinterpret_cast<const unsigned int*>(row + 8));
+        const uint32_t wv[5] = {v.x, v.y, v.z, v.w, nx};
+#pragma unroll
+        for (int u = 0; u < 5; ++u) {
+          if (P.storage == STORE_F16) {
+            s[2 * u] = half_bits_to_float(wv[u] & 0xffffu) * sc;
+            s[2 * u + 1] = half_bits_to_float(wv[u] >> 16) * sc;
+          } else {
+            s[2 * u] = __uint_as_float(wv[u] << 16) * sc;
+            s[2 * u + 1] = __uint_as_float(wv[u] & 0xffff0000u) * sc;
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) dst[8 * q + u] = make_float4(s[u], s[u + 1] - s[u], s[u + 1], s[u + 2] - s[u + 1]);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
-// item arithmetic
+// item state
 
 template <int W>
 struct PlainAcc {
@@ -302,12 +354,19 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
   ChunkMeta* meta = reinterpret_cast<ChunkMeta*>(smem_raw + 64);
   int4* srcinfo = reinterpret_cast<int4*>(smem_raw + 64 + ((sizeof(ChunkMeta) + 127) / 128) * 128);
   float* buf = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(srcinfo) + kMaxChunk * sizeof(int4));
+  float4* bufq = reinterpret_cast<float4*>(buf);
 
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
   constexpr float kSent = (METHOD == METHOD_CMP) ? -1.0f : 0.0f;
 
+  // zero block read by out-of-range items
+  if (FORM == FORM_PLAIN) {
+    if (threadIdx.x < kZeroSlots) buf[P.cap + threadIdx.x] = 0.f;
+  } else {
+    if (threadIdx.x < kZeroSlots) bufq[P.cap + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   if (threadIdx.x == 0 && FORM == FORM_PLAIN) {
     mbar_init(bar, 1);
     fence_mbar_init();
@@ -342,11 +401,11 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
     const float T_hi = P.dt * (float)t0hi;
 
     // per-thread running pick for this lane's t0
-    float best_s[FORM == FORM_FAST ? kTopK : 1];
-    int best_i[FORM == FORM_FAST ? kTopK : 1];
-    float best_k[FORM == FORM_FAST ? kTopK : 1];
+    constexpr int K = (FORM == FORM_FAST) ? kTopK : 1;
+    float best_s[K], best_k[K];
+    int best_i[K];
 #pragma unroll
-    for (int q = 0; q < (FORM == FORM_FAST ? kTopK : 1); ++q) {
+    for (int q = 0; q < K; ++q) {
       best_s[q] = 0.f;
       best_i[q] = 0x7fffffff;
       best_k[q] = 0.f;
@@ -359,35 +418,33 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
     const float T2smp = Tsmp * Tsmp;
     const float tau_lo = (float)P.tau;
     const float tau_hi = (float)(P.ns - P.tau - 1);
+    const unsigned span = (unsigned)(P.ns - 2 * P.tau - 2);   // valid iff 0 <= it - tau <= span
 
     for (int pass = 0; pass < P.npass; ++pass) {
       const float* pb = P.pass_bounds + pass * 8;
+      const float4* cand = P.cand + pass * P.cpp + warp * RC;
       float ca[RC], cb[RC], cc[RC];
-      int ci[RC];
 #pragma unroll
       for (int r = 0; r < RC; ++r) {
-        float4 cv = P.cand[pass * P.cpp + warp * RC + r];
+        const float4 cv = cand[r];
         ca[r] = cv.x;
         cb[r] = cv.y;
         cc[r] = cv.z;
-        ci[r] = __float_as_int(cv.w);
       }
       PlainAcc<W> pa[FORM == FORM_PLAIN ? RC : 1];
       FastAcc<W> fa[FORM == FORM_FAST ? RC : 1];
-      if (FORM == FORM_PLAIN) {
 #pragma unroll
-        for (int r = 0; r < RC; ++r) {
+      for (int r = 0; r < RC; ++r) {
 #pragma unroll
-          for (int j = 0; j < W; ++j) pa[r].num[j] = 0.f;
+        for (int j = 0; j < W; ++j) {
+          if (FORM == FORM_PLAIN) pa[r].num[j] = 0.f;
+          else fa[r].num[j] = 0.f;
+        }
+        if (FORM == FORM_PLAIN) {
           pa[r].den = 0.f;
           pa[r].lin = 0.f;
           pa[r].M = 0;
-        }
-      } else {
-#pragma unroll
-        for (int r = 0; r < RC; ++r) {
-#pragma unroll
-          for (int j = 0; j < W; ++j) fa[r].num[j] = 0.f;
+        } else {
           fa[r].den_c = 0.f;
           fa[r].den_hi = 0.f;
           fa[r].den_lo = 0.f;
@@ -421,40 +478,10 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
             return;
           }
         } else {
-          // cooperative copy: 16-bit or FP32 store -> FP32 x scale in shared memory
-          for (int e = warp; e < n; e += nwarps) {
-            int4 si = srcinfo[e];   // (trace, lo, len, off)
-            if (si.z <= 0) continue;
-            float* dst = buf + si.w;
-            if (P.storage == STORE_F32) {
-              const float4* src = reinterpret_cast<const float4*>(P.samples + (int64_t)si.x * P.pitch + si.y);
-              for (int q = lane; q < (si.z >> 2); q += 32) reinterpret_cast<float4*>(dst)[q] = __ldg(src + q);
-            } else {
-              const float sc = __ldg(P.scale + si.x);
-              const uint4* src = reinterpret_cast<const uint4*>(P.samples16 + (int64_t)si.x * P.pitch + si.y);
-              for (int q = lane; q < (si.z >> 3); q += 32) {
-                uint4 v = __ldg(src + q);
-                uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-                float o[8];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                  if (P.storage == STORE_F16) {
-                    o[2 * u] = half_bits_to_float(wv[u] & 0xffffu) * sc;
-                    o[2 * u + 1] = half_bits_to_float(wv[u] >> 16) * sc;
-                  } else {
-                    o[2 * u] = __uint_as_float(wv[u] << 16) * sc;
-                    o[2 * u + 1] = __uint_as_float(wv[u] & 0xffff0000u) * sc;
-                  }
-                }
-                reinterpret_cast<float4*>(dst)[2 * q] = make_float4(o[0], o[1], o[2], o[3]);
-                reinterpret_cast<float4*>(dst)[2 * q + 1] = make_float4(o[4], o[5], o[6], o[7]);
-              }
-            }
-          }
+          stage_fast(P, n, srcinfo, bufq);
           __syncthreads();
         }
 
-        const unsigned clamp_hi = (unsigned)(P.cap - W - 1);
         for (int e = 0; e < n; ++e) {
           const float4 g = meta->geo[e];
           const int soff = __float_as_int(g.w);
@@ -470,28 +497,25 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
                 t = (t < 0.0f) ? -1.0f : __fsqrt_rn(t);
                 t = __fmul_rn(t, P.idt);
               }
-              if (t >= tau_lo && t < tau_hi) {
-                const float y = __fadd_rz(t, 8388608.0f);
-                const int it = __float_as_int(y) - 0x4B000000;
-                const float x = __fsub_rn(t, __fsub_rn(y, 8388608.0f));
-                unsigned idx = (unsigned)(soff + it - P.tau);
-                idx = min(idx, clamp_hi);
-                const float* s = buf + idx;
-                float s1 = s[0];
+              const bool ok = (t >= tau_lo) && (t < tau_hi);
+              const float y = __fadd_rz(t, 8388608.0f);
+              const int it = __float_as_int(y) - 0x4B000000;
+              const float x = ok ? __fsub_rn(t, __fsub_rn(y, 8388608.0f)) : 0.0f;
+              const unsigned idx = min(ok ? (unsigned)(soff + it - P.tau) : (unsigned)P.cap, (unsigned)P.cap);
+              const float* s = buf + idx;
+              float s1 = s[0];
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                  const float s0 = s1;
-                  s1 = s[j + 1];
-                  const float v = __fadd_rn(__fmul_rn(__fsub_rn(s1, s0), x), s0);
-                  pa[r].num[j] = __fadd_rn(pa[r].num[j], v);
-                  pa[r].den = __fadd_rn(pa[r].den, __fmul_rn(v, v));
-                  pa[r].lin = __fadd_rn(pa[r].lin, v);
-                }
-                pa[r].M += 1;
+              for (int j = 0; j < W; ++j) {
+                const float s0 = s1;
+                s1 = s[j + 1];
+                const float v = __fadd_rn(__fmul_rn(__fsub_rn(s1, s0), x), s0);
+                pa[r].num[j] = __fadd_rn(pa[r].num[j], v);
+                pa[r].den = __fadd_rn(pa[r].den, __fmul_rn(v, v));
+                pa[r].lin = __fadd_rn(pa[r].lin, v);
               }
+              pa[r].M += ok ? 1 : 0;
             }
           } else {
-            const unsigned span = (unsigned)(P.ns - 2 * P.tau - 2);
 #pragma unroll
             for (int r = 0; r < RC; ++r) {
               float t2;
@@ -501,24 +525,30 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
                 const float u = fmaf(ca[r], g.x, Tsmp);
                 t2 = fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
               }
-              const float t = sqrt_fast(t2);
+              const float t = sqrt_fast(t2);   // NaN for t2 < 0: out of range below
               const float y = __fadd_rz(t, 8388608.0f);
               const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
-              if ((unsigned)rel <= span) {
-                const float x = t - (y - 8388608.0f);
-                unsigned idx = min((unsigned)(soff + rel), clamp_hi);
-                const float* s = buf + idx;
-                float s1 = s[0];
+              const bool ok = (unsigned)rel <= span;
+              const float x = ok ? t - (y - 8388608.0f) : 0.0f;
+              const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
+              const float4* q = bufq + idx;
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                  const float s0 = s1;
-                  s1 = s[j + 1];
-                  const float v = fmaf(s1 - s0, x, s0);
-                  fa[r].num[j] += v;
-                  fa[r].den_c = fmaf(v, v, fa[r].den_c);
-                }
-                fa[r].M += 1;
+              for (int p = 0; p < W / 2; ++p) {
+                const float4 ev = q[2 * p];
+                const float v0 = fmaf(ev.y, x, ev.x);
+                const float v1 = fmaf(ev.w, x, ev.z);
+                fa[r].num[2 * p] += v0;
+                fa[r].num[2 * p + 1] += v1;
+                fa[r].den_c = fmaf(v0, v0, fa[r].den_c);
+                fa[r].den_c = fmaf(v1, v1, fa[r].den_c);
               }
+              if (W & 1) {
+                const float2 ev = *reinterpret_cast<const float2*>(q + (W - 1));
+                const float v = fmaf(ev.y, x, ev.x);
+                fa[r].num[W - 1] += v;
+                fa[r].den_c = fmaf(v, v, fa[r].den_c);
+              }
+              fa[r].M += ok ? 1 : 0;
             }
           }
         }
@@ -564,30 +594,22 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
           sem = ok ? __fdividef(acsq, den * mf) : kSent;
           stk = ok ? __fdividef(lin, (float)W * mf) : kSent;
         }
-        const int idx = ci[r];
-        if (FORM == FORM_PLAIN) {
-          if (sem > 0.f && better(sem, idx, best_s[0], best_i[0])) {
-            best_s[0] = sem;
-            best_i[0] = idx;
-            best_k[0] = stk;
-          }
-        } else {
-          // sorted insert into the top-4 (descending semblance, ascending index)
-          if (sem > 0.f && better(sem, idx, best_s[kTopK - 1], best_i[kTopK - 1])) {
-            float cs = sem, ck = stk;
-            int cidx = idx;
+        const int idx = __float_as_int(cand[r].w);
+        if (sem > 0.f && better(sem, idx, best_s[K - 1], best_i[K - 1])) {
+          // sorted insert (descending semblance, ascending index)
+          float cs = sem, ck = stk;
+          int cidx = idx;
 #pragma unroll
-            for (int q = 0; q < kTopK; ++q) {
-              if (better(cs, cidx, best_s[q], best_i[q])) {
-                const float ts = best_s[q], tk = best_k[q];
-                const int ti = best_i[q];
-                best_s[q] = cs;
-                best_i[q] = cidx;
-                best_k[q] = ck;
-                cs = ts;
-                cidx = ti;
-                ck = tk;
-              }
+          for (int q = 0; q < K; ++q) {
+            if (better(cs, cidx, best_s[q], best_i[q])) {
+              const float ts = best_s[q], tk = best_k[q];
+              const int ti = best_i[q];
+              best_s[q] = cs;
+              best_i[q] = cidx;
+              best_k[q] = ck;
+              cs = ts;
+              cidx = ti;
+              ck = tk;
             }
           }
         }
@@ -596,7 +618,6 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
 
     // reduce the picks of all warps for each t0 (lane) through shared memory
     __syncthreads();
-    constexpr int K = (FORM == FORM_FAST) ? kTopK : 1;
     float* rs = buf;                                   // [nwarps][32][K]
     int* ri = reinterpret_cast<int*>(buf + nwarps * 32 * K);
     float* rk = buf + 2 * nwarps * 32 * K;

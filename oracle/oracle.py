@@ -47,12 +47,12 @@ def lib():
         for sfx in ("_f32", "_f64"):
             f = getattr(_lib, "semb_oracle_cmp" + sfx)
             f.restype = i32
-            f.argtypes = [i32, P, i32, i32, P, P, P, P, P, P, f64, f64, i32, f64, P, P, P, P, P, P]
+            f.argtypes = [i32, P, i32, i32, P, P, P, P, P, P, f64, f64, i32, f64, P, P, P, P, P, P, P, i32]
             f = getattr(_lib, "semb_oracle_crs" + sfx)
             f.restype = i32
             f.argtypes = [i32, P, i32, i32, P, P, P, P, P, P, P, P,
                           f64, f64, i32, f64, f64, i32, f64, f64, i32, f64,
-                          P, P, P, P, P, P, P, P, P]
+                          P, P, P, P, P, P, P, P, P, P, i32]
         _lib.semb_oracle_max_threads.restype = i32
         _lib.semb_oracle_set_threads.argtypes = [i32]
     return _lib
@@ -130,7 +130,16 @@ def gather(headers: np.ndarray, samples: np.ndarray, method: str, aph: int, apm:
     return g
 
 
-def cmp(g: dict, params: dict, precision: str = "f32", sem_all: bool = False, threads: int = 0) -> dict:
+def _list(cdps):
+    if cdps is None:
+        return None, 0
+    a = np.ascontiguousarray(cdps, dtype=np.int32)
+    return a, len(a)
+
+
+def cmp(g: dict, params: dict, precision: str = "f32", sem_all: bool = False, threads: int = 0,
+        cdps=None) -> dict:
+    """CMP search of the gather (all CDPs, or only the CDP indices in `cdps`)."""
     L = lib()
     if threads:
         L.semb_oracle_set_threads(threads)
@@ -143,11 +152,12 @@ def cmp(g: dict, params: dict, precision: str = "f32", sem_all: bool = False, th
     outc = np.zeros(ncdp * ns, np.float32)
     sem = np.zeros(ncdp * ns * nc, real) if sem_all else None
     secs = np.zeros(1, np.float64)
+    lst, nlst = _list(cdps)
     fn = getattr(L, "semb_oracle_cmp_" + precision)
     rc = fn(ncdp, _p(g["ntraces_by_cdp_id"]), ns, g["dt_us"], _p(g["samples"]),
             _p(g["gx"]), _p(g["gy"]), _p(g["sx"]), _p(g["sy"]), _p(g["scalco"]),
             parsed("cmp", params["c0"]), parsed("cmp", params["c1"]), nc, parsed("cmp", params["tau"]),
-            _p(ctr), _p(strr), _p(stk), _p(outc), _p(sem), _p(secs))
+            _p(ctr), _p(strr), _p(stk), _p(outc), _p(sem), _p(secs), _p(lst), nlst)
     if rc != 0:
         raise RuntimeError(f"oracle cmp failed: {rc}")
     out = dict(ctr=ctr.reshape(ncdp, ns), str=strr.reshape(ncdp, ns), stk=stk.reshape(ncdp, ns),
@@ -157,7 +167,10 @@ def cmp(g: dict, params: dict, precision: str = "f32", sem_all: bool = False, th
     return out
 
 
-def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, threads: int = 0) -> dict:
+def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, threads: int = 0,
+        cdps=None) -> dict:
+    """CRS search of the gather (all CDPs, or only the CDP indices in `cdps`, with
+    the neighbour lists of the whole gather)."""
     L = lib()
     if threads:
         L.semb_oracle_set_threads(threads)
@@ -173,12 +186,13 @@ def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, th
     secs = np.zeros(1, np.float64)
     nsem = np.zeros(1, np.int64)
     P = lambda k: parsed("crs", params[k])
+    lst, nlst = _list(cdps)
     fn = getattr(L, "semb_oracle_crs_" + precision)
     rc = fn(ncdp, _p(g["ntraces_by_cdp_id"]), ns, g["dt_us"], _p(g["samples"]),
             _p(g["gx"]), _p(g["gy"]), _p(g["sx"]), _p(g["sy"]), _p(g["scalco"]),
             _p(g["nbr_off"]), _p(g["nbr"]),
             P("a0"), P("a1"), na, P("b0"), P("b1"), nb, P("c0"), P("c1"), nc, P("tau"),
-            _p(ctr), _p(strr), _p(stk), _p(oa), _p(ob), _p(oc), _p(sem), _p(secs), _p(nsem))
+            _p(ctr), _p(strr), _p(stk), _p(oa), _p(ob), _p(oc), _p(sem), _p(secs), _p(nsem), _p(lst), nlst)
     if rc != 0:
         raise RuntimeError(f"oracle crs failed: {rc}")
     out = dict(ctr=ctr.reshape(ncdp, ns), str=strr.reshape(ncdp, ns), stk=stk.reshape(ncdp, ns),

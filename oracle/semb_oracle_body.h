@@ -15,6 +15,10 @@
  * Parameters are passed as the values the reference's parser produced: stof()
  * results for CMP, stod() results for CRS, both widened to double.
  *
+ * cdp_list (optional, n_list entries) restricts the search to those CDPs; the
+ * neighbour lists and geometry still come from the whole gather.  Rows of CDPs
+ * not in the list are left as the caller initialised them.
+ *
  * Divergence (documented): where the reference converts a NaN or out-of-int-range
  * traveltime with (int)t, which is undefined behaviour in C (x86 gives INT_MIN and
  * the window test then depends on signed overflow; AArch64 saturates), this
@@ -38,7 +42,7 @@ int CAT(semb_oracle_cmp, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
                               const int32_t* sxi, const int32_t* syi, const int32_t* scalcoi,
                               double c0_parsed, double c1_parsed, int nc, double tau_parsed,
                               int32_t* ctr, REAL* str, REAL* stk, float* out_c,
-                              REAL* sem_all, double* seconds) {
+                              REAL* sem_all, double* seconds, const int32_t* cdp_list, int n_list) {
   const REAL c0 = (REAL)(c0_parsed * FACTOR);
   const REAL c1 = (REAL)(c1_parsed * FACTOR);
   const REAL itau = (REAL)tau_parsed;
@@ -72,7 +76,9 @@ int CAT(semb_oracle_cmp, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
     h[i] = 0.25 * (hx * hx + hy * hy) / FACTOR;
   }
 
-  for (int cdp_id = 0; cdp_id < ncdps; cdp_id++) {
+  const int n_todo = cdp_list ? n_list : ncdps;
+  for (int q_id = 0; q_id < n_todo; q_id++) {
+    const int cdp_id = cdp_list ? cdp_list[q_id] : q_id;
     const int t_id0 = cdp_id > 0 ? ntraces_by_cdp_id[cdp_id - 1] : 0;
     const int t_idf = ntraces_by_cdp_id[cdp_id];
     const float* cdpsmpl = samples + (size_t)t_id0 * ns;
@@ -158,7 +164,8 @@ int CAT(semb_oracle_crs, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
                               double c0_parsed, double c1_parsed, int nc, double tau_parsed,
                               int32_t* ctr, REAL* str, REAL* stk,
                               float* out_a, float* out_b, float* out_c,
-                              REAL* sem_all, double* seconds, int64_t* n_semblance_traces) {
+                              REAL* sem_all, double* seconds, int64_t* n_semblance_traces,
+                              const int32_t* cdp_list, int n_list) {
   const REAL a0 = (REAL)a0_parsed, a1 = (REAL)a1_parsed;
   const REAL b0 = (REAL)b0_parsed, b1 = (REAL)b1_parsed;
   const REAL c0 = (REAL)(c0_parsed * FACTOR), c1 = (REAL)(c1_parsed * FACTOR);
@@ -227,7 +234,9 @@ int CAT(semb_oracle_crs, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
     h0[i] = 0.25 * (hx * hx + hy * hy) / FACTOR;
   }
 
-  for (int cdp_id = 0; rc == 0 && cdp_id < ncdps; cdp_id++) {
+  const int n_todo = cdp_list ? n_list : ncdps;
+  for (int q_id = 0; rc == 0 && q_id < n_todo; q_id++) {
+    const int cdp_id = cdp_list ? cdp_list[q_id] : q_id;
     const int first = cdp_id > 0 ? ntraces_by_cdp_id[cdp_id - 1] : 0;
     const REAL m0x_cdp_id = m0x[first], m0y_cdp_id = m0y[first];
     int size = 0;
