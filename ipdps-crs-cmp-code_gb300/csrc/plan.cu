@@ -544,7 +544,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
 
   // staging capacity: as large as two resident CTAs per SM allow (about 113 KB of
   // shared memory each), and never less than one whole trace
-  const size_t fixed = 64 + ((sizeof(ChunkMeta) + 127) / 128) * 128 + kMaxChunk * sizeof(int4);
+  const size_t fixed = smem_fixed_bytes(form == FORM_FAST ? kTopK : 1) + kahan_bytes(form, rc);
   const size_t unit = form == FORM_PLAIN ? sizeof(float) : sizeof(float4);
   const size_t budget = 113 * 1024 - fixed - kZeroSlots * unit;
   int cap = (int)(budget / unit) & ~7;

@@ -35,9 +35,10 @@
 //          and division, the same `lin` accumulator; staged by 1-D bulk copies
 //          (TMA) of the FP32 trace store.  Bit-compatible with the reference's
 //          single-precision build.
-//   FAST   traces stored as FP16/BF16 (+ FP32 scale) or FP32, staged as 16-byte
-//          entries (s_k, s_k+1 - s_k, s_k+1, s_k+2 - s_k+1) so that a w-sample
-//          window is ceil(w/2) vector loads and one FMA per interpolated sample;
+//   FAST   traces stored as FP16/BF16 (+ FP32 scale) or FP32, staged as FP32
+//          16-byte entries (s_k, s_k+1, s_k+2, s_k+3), one per sample, so that the
+//          w+1 samples of a window are ceil((w+1)/4) vector loads (w = 3: one
+//          LDS.128, 16 bytes; w = 5: LDS.128 + LDS.64, 24 bytes);
 //          FP32 arithmetic with fused multiply-adds and hardware sqrt, traveltimes
 //          in sample units (candidates pre-scaled by idt), the stack taken from
 //          sum_j num_j, and the energy accumulated per chunk and folded into a
@@ -60,6 +61,7 @@ constexpr int kMaxChunk = 128;   // aperture traces staged per chunk
 constexpr int kMargin = 2;       // extra samples on each side of a staged window
 constexpr int kTopK = 4;
 constexpr int kZeroSlots = 16;   // zero block after the staging buffer (floats or entries)
+constexpr int kMaxThreads = 256; // CTA size limit of the search kernel
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier wait (2 s), then error
 
 // Device status word bits.
@@ -170,16 +172,26 @@ __device__ __forceinline__ bool better(float s, int i, float bs, int bi) {
 
 struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
+  int inrange[kMaxChunk];  // 1 when every item of the pass is in range on this trace
   int n;                   // entries in this chunk
   int bytes;               // bytes staged (TMA form)
 };
+
+constexpr size_t kMetaBytes = ((sizeof(ChunkMeta) + 127) / 128) * 128;
+
+// Shared memory in front of the staging buffer (bytes): barrier and control
+// words, chunk metadata, copy descriptors and the per-thread top-K lists.
+__host__ __device__ constexpr size_t smem_fixed_bytes(int K) {
+  return 64 + kMetaBytes + kMaxChunk * sizeof(int4) + 3 * (size_t)K * kMaxThreads * 4;
+}
 
 // Sample window [lo, hi] of one trace that items of a pass can read, for t0 in
 // [T_lo, T_hi] (seconds) and parameters within the pass bounds.  Returns false
 // when no item can be in range.
 template <int METHOD>
 __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_lo, float T_hi, float idt,
-                                             int tau, int ns, int& lo, int& hi) {
+                                             int tau, int ns, int& lo, int& hi, bool& inrange) {
+  inrange = false;
   float t2min, t2max;
   if (METHOD == METHOD_CMP) {
     // t^2 = t0^2 + c*h, h >= 0
@@ -207,6 +219,8 @@ __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_
   float smax = sqrtf(t2max) * idt;
   smin = fminf(smin, (float)ns + 8.f);
   smax = fminf(smax, (float)ns + 8.f);
+  // in range for sure: tau <= it <= ns - tau - 2 for every item, with one sample of slack
+  inrange = t2min > 0.f && smin >= (float)(tau + 1) && smax <= (float)(ns - tau - 3);
   lo = (int)smin - tau - kMargin;
   hi = (int)smax + tau + 1 + kMargin;
   lo = max(lo, 0);
@@ -233,9 +247,10 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
     float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
     int lo = 0, hi = -1;
     int len = 0;
+    bool inr = false;
     if (have) {
       g = P.ap_geo[k];
-      if (trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi)) {
+      if (trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi, inr)) {
         lo &= ~(ALIGN - 1);
         hi |= (ALIGN - 1);
         len = hi - lo + 1;
@@ -254,6 +269,7 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
       const int off = base + incl - len;
       g.w = __int_as_float(off - lo);
       meta->geo[n + lane] = g;
+      meta->inrange[n + lane] = (FORM == FORM_FAST && inr) ? 1 : 0;
       src[n + lane] = make_int4(P.ap_tr[k], lo, len, off);
     }
     base += nfit > 0 ? __shfl_sync(0xffffffffu, incl, nfit - 1) : 0;
@@ -281,46 +297,60 @@ __device__ __forceinline__ void issue_chunk_copies(const KParams& P, ChunkMeta* 
   }
 }
 
-// Fast form: all warps turn the chunk's windows into (s, ds) entries.  Each lane
-// handles 8 samples at a time (one 16-byte load of 16-bit samples, or two of FP32)
-// plus the 2 samples after them for the differences.
+// Fast form: all warps turn the chunk's windows into quad entries.  Lane l of a
+// warp builds entry k = k0 + l from samples k..k+3 (four loads that the warp
+// coalesces and L1 serves), so each 16-byte store of the warp covers 512
+// consecutive bytes without bank conflicts.
+__device__ __forceinline__ float load_sample(const KParams& P, int64_t i, float sc) {
+  if (P.storage == STORE_F32) return __ldg(P.samples + i);
+  const uint32_t b = __ldg(P.samples16 + i);
+  return (P.storage == STORE_F16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
+}
+
 __device__ __forceinline__ void stage_fast(const KParams& P, int n, const int4* src, float4* bufq) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int e = warp; e < n; e += nwarps) {
     const int4 si = src[e];   // (trace, lo, len, off)
     if (si.z <= 0) continue;
+    const float sc = P.storage == STORE_F32 ? 1.0f : __ldg(P.scale + si.x);
+    const int64_t row = (int64_t)si.x * P.pitch + si.y;
     float4* dst = bufq + si.w;
-    const int groups = si.z >> 3;
-    float s[10];
-    for (int q = lane; q < groups; q += 32) {
-      if (P.storage == STORE_F32) {
-        const float* row = P.samples + (int64_t)si.x * P.pitch + si.y + 8 * q;
-        const float4 a = __ldg(reinterpret_cast<const float4*>(row));
-        const float4 b = __ldg(reinterpret_cast<const float4*>(row) + 1);
-        const float2 c = __ldg(reinterpret_cast<const float2*>(row + 8));
-        s[0] = a.x; s[1] = a.y; s[2] = a.z; s[3] = a.w;
-        s[4] = b.x; s[5] = b.y; s[6] = b.z; s[7] = b.w;
-        s[8] = c.x; s[9] = c.y;
-      } else {
-        const float sc = __ldg(P.scale + si.x);
-        const uint16_t* row = P.samples16 + (int64_t)si.x * P.pitch + si.y + 8 * q;
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(row));
-        const uint32_t nx = __ldg(reinterpret_cast<const unsigned int*>(row + 8));
-        const uint32_t wv[5] = {v.x, v.y, v.z, v.w, nx};
-#pragma unroll
-        for (int u = 0; u < 5; ++u) {
-          if (P.storage == STORE_F16) {
-            s[2 * u] = half_bits_to_float(wv[u] & 0xffffu) * sc;
-            s[2 * u + 1] = half_bits_to_float(wv[u] >> 16) * sc;
-          } else {
-            s[2 * u] = __uint_as_float(wv[u] << 16) * sc;
-            s[2 * u + 1] = __uint_as_float(wv[u] & 0xffff0000u) * sc;
-          }
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) dst[8 * q + u] = make_float4(s[u], s[u + 1] - s[u], s[u + 1], s[u + 2] - s[u + 1]);
+    for (int k = lane; k < si.z; k += 32) {
+      const int64_t i = row + k;
+      dst[k] = make_float4(load_sample(P, i, sc), load_sample(P, i + 1, sc), load_sample(P, i + 2, sc),
+                           load_sample(P, i + 3, sc));
     }
+  }
+}
+
+// Shared-memory vector loads at a 32-bit shared address.
+__device__ __forceinline__ float4 lds128(uint32_t a) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+  return v;
+}
+
+__device__ __forceinline__ float2 lds64(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  return v;
+}
+
+// Samples s[0..W] of a window starting at entry address `a` (quad layout).
+template <int W>
+__device__ __forceinline__ void load_window(uint32_t a, float (&sv)[W + 1]) {
+#pragma unroll
+  for (int i = 0; i < (W + 1) / 4; ++i) {
+    const float4 q = lds128(a + 64u * i);
+    sv[4 * i] = q.x;
+    sv[4 * i + 1] = q.y;
+    sv[4 * i + 2] = q.z;
+    sv[4 * i + 3] = q.w;
+  }
+  if ((W + 1) % 4 == 2) {
+    const float2 q = lds64(a + 64u * ((W + 1) / 4));
+    sv[W - 1] = q.x;
+    sv[W] = q.y;
   }
 }
 
@@ -337,24 +367,35 @@ struct PlainAcc {
 template <int W>
 struct FastAcc {
   float num[W];
-  float den_c;      // energy of the current chunk
-  float den_hi;     // Kahan-compensated total
-  float den_lo;     // compensation
-  int M;
+  float den_c;      // energy of the current chunk; the Kahan-compensated total
+  int M;            // and its compensation live in shared memory (kahan_hi/lo)
 };
+
+// Shared memory of the fast form's Kahan totals: [2][RC][kMaxThreads] floats.
+__host__ __device__ constexpr size_t kahan_bytes(int form, int rc) {
+  return form == FORM_FAST ? 2 * (size_t)rc * kMaxThreads * 4 : 0;
+}
 
 // ---------------------------------------------------------------------------
 // The search kernel.
 
 template <int METHOD, int FORM, int W, int RC>
-__global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
+__global__ void __launch_bounds__(kMaxThreads, 2) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   int* ctl = reinterpret_cast<int*>(smem_raw + 16);
   ChunkMeta* meta = reinterpret_cast<ChunkMeta*>(smem_raw + 64);
-  int4* srcinfo = reinterpret_cast<int4*>(smem_raw + 64 + ((sizeof(ChunkMeta) + 127) / 128) * 128);
-  float* buf = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(srcinfo) + kMaxChunk * sizeof(int4));
+  int4* srcinfo = reinterpret_cast<int4*>(smem_raw + 64 + kMetaBytes);
+  // running top-K per thread, [K][blockDim] (semblance, grid index, stack)
+  constexpr int K = (FORM == FORM_FAST) ? kTopK : 1;
+  float* top_s = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(srcinfo) + kMaxChunk * sizeof(int4));
+  int* top_i = reinterpret_cast<int*>(top_s + K * kMaxThreads);
+  float* top_k = top_s + 2 * K * kMaxThreads;
+  float* kahan_hi = top_s + 3 * K * kMaxThreads;   // fast form: [RC][kMaxThreads]
+  float* kahan_lo = kahan_hi + RC * kMaxThreads;
+  float* buf = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(kahan_hi) + kahan_bytes(FORM, RC));
   float4* bufq = reinterpret_cast<float4*>(buf);
+  const uint32_t bufq_addr = smem_u32(bufq);
 
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -400,16 +441,16 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
     const float T_lo = P.dt * (float)t0s;
     const float T_hi = P.dt * (float)t0hi;
 
-    // per-thread running pick for this lane's t0
-    constexpr int K = (FORM == FORM_FAST) ? kTopK : 1;
-    float best_s[K], best_k[K];
-    int best_i[K];
+    // per-thread running pick for this lane's t0: top-K in shared memory, the
+    // admission threshold (the K-th entry) in registers
 #pragma unroll
     for (int q = 0; q < K; ++q) {
-      best_s[q] = 0.f;
-      best_i[q] = 0x7fffffff;
-      best_k[q] = 0.f;
+      top_s[q * kMaxThreads + threadIdx.x] = 0.f;
+      top_i[q * kMaxThreads + threadIdx.x] = 0x7fffffff;
+      top_k[q * kMaxThreads + threadIdx.x] = 0.f;
     }
+    float last_s = 0.f;
+    int last_i = 0x7fffffff;
 
     // per-lane time values
     const float Tsec = __fmul_rn(P.dt, (float)t0);            // reference: _t0 = dt * t0
@@ -446,9 +487,9 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
           pa[r].M = 0;
         } else {
           fa[r].den_c = 0.f;
-          fa[r].den_hi = 0.f;
-          fa[r].den_lo = 0.f;
           fa[r].M = 0;
+          kahan_hi[r * kMaxThreads + threadIdx.x] = 0.f;
+          kahan_lo[r * kMaxThreads + threadIdx.x] = 0.f;
         }
       }
 
@@ -516,50 +557,65 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
               pa[r].M += ok ? 1 : 0;
             }
           } else {
+            // t2 in samples^2 for item r on this trace
+            auto t2_of = [&](int r) {
+              if (METHOD == METHOD_CMP) return fmaf(cc[r], g.z, T2smp);
+              const float u = fmaf(ca[r], g.x, Tsmp);
+              return fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
+            };
+            auto accumulate = [&](int r, uint32_t a, float x) {
+              float sv[W + 1];
+              load_window<W>(a, sv);
 #pragma unroll
-            for (int r = 0; r < RC; ++r) {
-              float t2;
-              if (METHOD == METHOD_CMP) {
-                t2 = fmaf(cc[r], g.z, T2smp);
-              } else {
-                const float u = fmaf(ca[r], g.x, Tsmp);
-                t2 = fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
-              }
-              const float t = sqrt_fast(t2);   // NaN for t2 < 0: out of range below
-              const float y = __fadd_rz(t, 8388608.0f);
-              const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
-              const bool ok = (unsigned)rel <= span;
-              const float x = ok ? t - (y - 8388608.0f) : 0.0f;
-              const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
-              const float4* q = bufq + idx;
-#pragma unroll
-              for (int p = 0; p < W / 2; ++p) {
-                const float4 ev = q[2 * p];
-                const float v0 = fmaf(ev.y, x, ev.x);
-                const float v1 = fmaf(ev.w, x, ev.z);
-                fa[r].num[2 * p] += v0;
-                fa[r].num[2 * p + 1] += v1;
-                fa[r].den_c = fmaf(v0, v0, fa[r].den_c);
-                fa[r].den_c = fmaf(v1, v1, fa[r].den_c);
-              }
-              if (W & 1) {
-                const float2 ev = *reinterpret_cast<const float2*>(q + (W - 1));
-                const float v = fmaf(ev.y, x, ev.x);
-                fa[r].num[W - 1] += v;
+              for (int j = 0; j < W; ++j) {
+                const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
+                fa[r].num[j] += v;
                 fa[r].den_c = fmaf(v, v, fa[r].den_c);
               }
-              fa[r].M += ok ? 1 : 0;
+            };
+            if (meta->inrange[e]) {
+              // every item in range: address = bits(t + 2^23) * 16 + base (mod 2^32),
+              // clamped to the buffer as a guard
+              const uint32_t base = bufq_addr + 16u * (uint32_t)(soff - P.tau) - 16u * 0x4B000000u;
+              const uint32_t top = bufq_addr + 16u * (uint32_t)P.cap;
+#pragma unroll
+              for (int r = 0; r < RC; ++r) {
+                const float t = sqrt_fast(t2_of(r));
+                const float y = __fadd_rz(t, 8388608.0f);
+                accumulate(r, min(__float_as_uint(y) * 16u + base, top), t - (y - 8388608.0f));
+              }
+            } else {
+#pragma unroll
+              for (int r = 0; r < RC; ++r) {
+                const float t = sqrt_fast(t2_of(r));   // NaN for t2 < 0: out of range below
+                const float y = __fadd_rz(t, 8388608.0f);
+                const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
+                const bool ok = (unsigned)rel <= span;
+                const float x = ok ? t - (y - 8388608.0f) : 0.0f;
+                const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
+                accumulate(r, bufq_addr + 16u * idx, x);
+                fa[r].M += ok ? 1 : 0;
+              }
             }
           }
+        }
+        if (FORM == FORM_FAST) {
+          // traces flagged in range count for every item
+          int ninr = 0;
+          for (int e = 0; e < n; ++e) ninr += meta->inrange[e];
+#pragma unroll
+          for (int r = 0; r < RC; ++r) fa[r].M += ninr;
         }
         if (FORM == FORM_FAST) {
 #pragma unroll
           for (int r = 0; r < RC; ++r) {
             // Kahan: fold this chunk's energy into the compensated total
-            const float yv = fa[r].den_c - fa[r].den_lo;
-            const float tv = fa[r].den_hi + yv;
-            fa[r].den_lo = (tv - fa[r].den_hi) - yv;
-            fa[r].den_hi = tv;
+            const int o = r * kMaxThreads + threadIdx.x;
+            const float hi = kahan_hi[o], lo = kahan_lo[o];
+            const float yv = fa[r].den_c - lo;
+            const float tv = hi + yv;
+            kahan_lo[o] = (tv - hi) - yv;
+            kahan_hi[o] = tv;
             fa[r].den_c = 0.f;
           }
         }
@@ -587,7 +643,7 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
             acsq = fmaf(fa[r].num[j], fa[r].num[j], acsq);
             lin += fa[r].num[j];
           }
-          const float den = fa[r].den_hi - fa[r].den_lo;
+          const float den = kahan_hi[r * kMaxThreads + threadIdx.x] - kahan_lo[r * kMaxThreads + threadIdx.x];
           const float mf = (float)fa[r].M;
           const int err = napert - fa[r].M;
           const bool ok = ((double)den > 1e-13) && (fa[r].M > 0) && (err < 2);
@@ -595,38 +651,33 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
           stk = ok ? __fdividef(lin, (float)W * mf) : kSent;
         }
         const int idx = __float_as_int(cand[r].w);
-        if (sem > 0.f && better(sem, idx, best_s[K - 1], best_i[K - 1])) {
+        if (sem > 0.f && better(sem, idx, last_s, last_i)) {
           // sorted insert (descending semblance, ascending index)
           float cs = sem, ck = stk;
           int cidx = idx;
 #pragma unroll
           for (int q = 0; q < K; ++q) {
-            if (better(cs, cidx, best_s[q], best_i[q])) {
-              const float ts = best_s[q], tk = best_k[q];
-              const int ti = best_i[q];
-              best_s[q] = cs;
-              best_i[q] = cidx;
-              best_k[q] = ck;
-              cs = ts;
-              cidx = ti;
-              ck = tk;
+            const int o = q * kMaxThreads + threadIdx.x;
+            const float bs = top_s[o];
+            const int bi = top_i[o];
+            if (better(cs, cidx, bs, bi)) {
+              const float bk = top_k[o];
+              top_s[o] = cs;
+              top_i[o] = cidx;
+              top_k[o] = ck;
+              cs = bs;
+              cidx = bi;
+              ck = bk;
             }
           }
+          last_s = top_s[(K - 1) * kMaxThreads + threadIdx.x];
+          last_i = top_i[(K - 1) * kMaxThreads + threadIdx.x];
         }
       }
     }
 
-    // reduce the picks of all warps for each t0 (lane) through shared memory
-    __syncthreads();
-    float* rs = buf;                                   // [nwarps][32][K]
-    int* ri = reinterpret_cast<int*>(buf + nwarps * 32 * K);
-    float* rk = buf + 2 * nwarps * 32 * K;
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-      rs[(warp * 32 + lane) * K + q] = best_s[q];
-      ri[(warp * 32 + lane) * K + q] = best_i[q];
-      rk[(warp * 32 + lane) * K + q] = best_k[q];
-    }
+    // reduce the picks of all warps for each t0 (lane): warp 0 reads every warp's
+    // lists from shared memory
     __syncthreads();
     if (warp == 0) {
       float fs[K], fk[K];
@@ -639,9 +690,9 @@ __global__ void __launch_bounds__(256, 2) semb_search_kernel(KParams P) {
       }
       for (int w2 = 0; w2 < nwarps; ++w2) {
         for (int q2 = 0; q2 < K; ++q2) {
-          float cs = rs[(w2 * 32 + lane) * K + q2];
-          int cidx = ri[(w2 * 32 + lane) * K + q2];
-          float ck = rk[(w2 * 32 + lane) * K + q2];
+          float cs = top_s[q2 * kMaxThreads + w2 * 32 + lane];
+          int cidx = top_i[q2 * kMaxThreads + w2 * 32 + lane];
+          float ck = top_k[q2 * kMaxThreads + w2 * 32 + lane];
           if (!(cs > 0.f)) continue;
 #pragma unroll
           for (int q = 0; q < K; ++q) {
