@@ -544,13 +544,13 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
 
   // staging capacity: as large as two resident CTAs per SM allow (about 113 KB of
   // shared memory each), and never less than one whole trace
-  const size_t fixed = smem_fixed_bytes(form == FORM_FAST ? kTopK : 1) + kahan_bytes(form, rc);
-  const size_t unit = form == FORM_PLAIN ? sizeof(float) : sizeof(float4);
-  const size_t budget = 113 * 1024 - fixed - kZeroSlots * unit;
-  int cap = (int)(budget / unit) & ~7;
-  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 7) & ~7;
+  const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
+  const size_t budget = 113 * 1024;
+  int cap = form == FORM_PLAIN ? 32768 : 8192;
+  while (cap > 64 && smem_layout(form, rc, cap, store).total > budget) cap -= 64;
+  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
   pl->cap = cap;
-  pl->smem = fixed + ((size_t)cap + kZeroSlots) * unit;
+  pl->smem = smem_layout(form, rc, cap, store).total;
   if (pl->smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", g->ns);
   SEMB_TRY(search_occupancy(p.method, form, pl->w, pl->nwarps, pl->smem, &pl->ctas_per_sm));
   if (pl->ctas_per_sm <= 0) return fail(SEMB_E_CUDA, "search kernel cannot be resident with %zu bytes", pl->smem);

@@ -173,16 +173,49 @@ __device__ __forceinline__ bool better(float s, int i, float bs, int bi) {
 struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
   int inrange[kMaxChunk];  // 1 when every item of the pass is in range on this trace
+  float scale[kMaxChunk];  // fast form: per-trace scale of the 16-bit store
   int n;                   // entries in this chunk
   int bytes;               // bytes staged (TMA form)
 };
 
 constexpr size_t kMetaBytes = ((sizeof(ChunkMeta) + 127) / 128) * 128;
 
-// Shared memory in front of the staging buffer (bytes): barrier and control
-// words, chunk metadata, copy descriptors and the per-thread top-K lists.
-__host__ __device__ constexpr size_t smem_fixed_bytes(int K) {
-  return 64 + kMetaBytes + kMaxChunk * sizeof(int4) + 3 * (size_t)K * kMaxThreads * 4;
+// Shared-memory layout of the search kernel (bytes), shared by host and device:
+//   [0, 64)   two mbarriers and control words
+//   meta[2]   chunk metadata (the fast form alternates two chunks)
+//   src[2]    per-entry copy descriptors (trace, first sample, length, offset)
+//   top-K     per-thread running picks [3][K][kMaxThreads]
+//   kahan     fast form: per-item compensated energy totals [2][RC][kMaxThreads]
+//   buf       staging buffer: cap floats (plain) or cap 16-byte quads (fast),
+//             followed by kZeroSlots zeroed slots read by out-of-range items
+//   raw[2]    fast form: the raw windows of two chunks as stored in HBM
+//             (16-bit or FP32), cap + 8*kMaxChunk samples each
+struct SmemLayout {
+  size_t meta, src, tops, kahan, buf, raw0, raw1, total;
+};
+
+__host__ __device__ inline size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
+
+__host__ __device__ inline SmemLayout smem_layout(int form, int rc, int cap, int storage) {
+  const int K = form == 1 ? 4 : 1;
+  SmemLayout L;
+  L.meta = 64;
+  L.src = L.meta + 2 * kMetaBytes;
+  L.tops = L.src + 2 * kMaxChunk * sizeof(int4);
+  L.kahan = L.tops + align128(3 * (size_t)K * kMaxThreads * 4);
+  L.buf = L.kahan + (form == 1 ? 2 * (size_t)rc * kMaxThreads * 4 : 0);
+  const size_t unit = form == 1 ? 16 : 4;
+  const size_t raw_end = L.buf + align128(((size_t)cap + kZeroSlots) * unit);
+  if (form == 1) {
+    const size_t rb = align128(((size_t)cap + 8 * kMaxChunk) * (storage == 0 ? 4 : 2));
+    L.raw0 = raw_end;
+    L.raw1 = raw_end + rb;
+    L.total = raw_end + 2 * rb;
+  } else {
+    L.raw0 = L.raw1 = raw_end;
+    L.total = raw_end;
+  }
+  return L;
 }
 
 // Sample window [lo, hi] of one trace that items of a pass can read, for t0 in
@@ -248,8 +281,12 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
     int lo = 0, hi = -1;
     int len = 0;
     bool inr = false;
+    int tr = 0;
+    float sc = 1.0f;
     if (have) {
       g = P.ap_geo[k];
+      tr = P.ap_tr[k];
+      if (FORM == FORM_FAST && P.storage != STORE_F32) sc = __ldg(P.scale + tr);
       if (trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi, inr)) {
         lo &= ~(ALIGN - 1);
         hi |= (ALIGN - 1);
@@ -270,7 +307,8 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
       g.w = __int_as_float(off - lo);
       meta->geo[n + lane] = g;
       meta->inrange[n + lane] = (FORM == FORM_FAST && inr) ? 1 : 0;
-      src[n + lane] = make_int4(P.ap_tr[k], lo, len, off);
+      meta->scale[n + lane] = sc;
+      src[n + lane] = make_int4(tr, lo, len, off);
     }
     base += nfit > 0 ? __shfl_sync(0xffffffffu, incl, nfit - 1) : 0;
     n += nfit;
@@ -280,6 +318,7 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
     meta->n = n;
     meta->bytes = base * 4;
   }
+  __syncwarp();
 }
 
 // Warp 0, after plan_chunk (plain form): announce the chunk's bytes on the
@@ -297,30 +336,73 @@ __device__ __forceinline__ void issue_chunk_copies(const KParams& P, ChunkMeta* 
   }
 }
 
-// Fast form: all warps turn the chunk's windows into quad entries.  Lane l of a
-// warp builds entry k = k0 + l from samples k..k+3 (four loads that the warp
-// coalesces and L1 serves), so each 16-byte store of the warp covers 512
-// consecutive bytes without bank conflicts.
-__device__ __forceinline__ float load_sample(const KParams& P, int64_t i, float sc) {
-  if (P.storage == STORE_F32) return __ldg(P.samples + i);
-  const uint32_t b = __ldg(P.samples16 + i);
-  return (P.storage == STORE_F16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
+// Fast form, warp 0 after plan_chunk: start one bulk copy (TMA) per staged window
+// of the raw store into `raw`, each window plus the 8 samples after it (the quads
+// of the last samples read 3 past the window).  Entry e lands at raw offset
+// off_e + 8e samples.  The barrier is told the total bytes first.
+__device__ __forceinline__ void issue_raw(const KParams& P, const ChunkMeta* meta, const int4* src,
+                                          unsigned char* raw, uint64_t* bar) {
+  const int lane = threadIdx.x & 31;
+  const int n = meta->n;
+  const uint32_t unit = P.storage == STORE_F32 ? 4u : 2u;
+  uint32_t bytes = 0;
+  for (int e = lane; e < n; e += 32) {
+    const int4 si = src[e];
+    if (si.z > 0) bytes += (uint32_t)(si.z + 8) * unit;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+  if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+  __syncwarp();
+  for (int e = lane; e < n; e += 32) {
+    const int4 si = src[e];
+    if (si.z <= 0) continue;
+    const int64_t at = (int64_t)si.x * P.pitch + si.y;
+    const void* g = P.storage == STORE_F32 ? (const void*)(P.samples + at) : (const void*)(P.samples16 + at);
+    bulk_g2s(raw + (size_t)(si.w + 8 * e) * unit, g, (uint32_t)(si.z + 8) * unit, bar);
+  }
 }
 
-__device__ __forceinline__ void stage_fast(const KParams& P, int n, const int4* src, float4* bufq) {
+// Fast form, all warps: turn the landed raw windows into quad entries.  Lane l
+// builds entry k = k0 + l from raw samples k..k+3, so the warp's 16-byte stores
+// cover consecutive addresses (no bank conflicts).
+__device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta* meta, const int4* src,
+                                              const unsigned char* raw, float4* bufq) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int n = meta->n;
   for (int e = warp; e < n; e += nwarps) {
     const int4 si = src[e];   // (trace, lo, len, off)
     if (si.z <= 0) continue;
-    const float sc = P.storage == STORE_F32 ? 1.0f : __ldg(P.scale + si.x);
-    const int64_t row = (int64_t)si.x * P.pitch + si.y;
     float4* dst = bufq + si.w;
-    for (int k = lane; k < si.z; k += 32) {
-      const int64_t i = row + k;
-      dst[k] = make_float4(load_sample(P, i, sc), load_sample(P, i + 1, sc), load_sample(P, i + 2, sc),
-                           load_sample(P, i + 3, sc));
+    const int roff = si.w + 8 * e;
+    if (P.storage == STORE_F32) {
+      const float* r = reinterpret_cast<const float*>(raw) + roff;
+      for (int k = lane; k < si.z; k += 32) dst[k] = make_float4(r[k], r[k + 1], r[k + 2], r[k + 3]);
+    } else {
+      const float sc = meta->scale[e];
+      const uint16_t* r = reinterpret_cast<const uint16_t*>(raw) + roff;
+      const bool f16 = P.storage == STORE_F16;
+      for (int k = lane; k < si.z; k += 32) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint32_t b = r[k + u];
+          v[u] = (f16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
+        }
+        dst[k] = make_float4(v[0], v[1], v[2], v[3]);
+      }
     }
   }
+}
+
+// Bounded wait on a barrier phase; false when it did not complete within kWaitNs.
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t_start = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t_start > kWaitNs) return false;
+  }
+  return true;
 }
 
 // Shared-memory vector loads at a 32-bit shared address.
@@ -382,20 +464,26 @@ __host__ __device__ constexpr size_t kahan_bytes(int form, int rc) {
 template <int METHOD, int FORM, int W, int RC>
 __global__ void __launch_bounds__(kMaxThreads, 2) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);   // [2]
   int* ctl = reinterpret_cast<int*>(smem_raw + 16);
-  ChunkMeta* meta = reinterpret_cast<ChunkMeta*>(smem_raw + 64);
-  int4* srcinfo = reinterpret_cast<int4*>(smem_raw + 64 + kMetaBytes);
-  // running top-K per thread, [K][blockDim] (semblance, grid index, stack)
+  ChunkMeta* metas = reinterpret_cast<ChunkMeta*>(smem_raw + L.meta);   // [2], stride kMetaBytes
+  int4* srcs = reinterpret_cast<int4*>(smem_raw + L.src);               // [2][kMaxChunk]
+  // running top-K per thread, [K][kMaxThreads] (semblance, grid index, stack)
   constexpr int K = (FORM == FORM_FAST) ? kTopK : 1;
-  float* top_s = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(srcinfo) + kMaxChunk * sizeof(int4));
+  float* top_s = reinterpret_cast<float*>(smem_raw + L.tops);
   int* top_i = reinterpret_cast<int*>(top_s + K * kMaxThreads);
   float* top_k = top_s + 2 * K * kMaxThreads;
-  float* kahan_hi = top_s + 3 * K * kMaxThreads;   // fast form: [RC][kMaxThreads]
+  float* kahan_hi = reinterpret_cast<float*>(smem_raw + L.kahan);   // fast form: [RC][kMaxThreads]
   float* kahan_lo = kahan_hi + RC * kMaxThreads;
-  float* buf = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(kahan_hi) + kahan_bytes(FORM, RC));
+  float* buf = reinterpret_cast<float*>(smem_raw + L.buf);
   float4* bufq = reinterpret_cast<float4*>(buf);
+  auto raw_at = [&](int i) { return smem_raw + L.raw0 + (size_t)i * (L.raw1 - L.raw0); };
   const uint32_t bufq_addr = smem_u32(bufq);
+  auto meta_at = [&](int i) { return reinterpret_cast<ChunkMeta*>(reinterpret_cast<unsigned char*>(metas) + i * kMetaBytes); };
+  ChunkMeta* meta = meta_at(0);
+  int4* srcinfo = srcs;
+  uint64_t* bar = bars;
 
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -408,12 +496,14 @@ __global__ void __launch_bounds__(kMaxThreads, 2) semb_search_kernel(KParams P) 
   } else {
     if (threadIdx.x < kZeroSlots) bufq[P.cap + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  if (threadIdx.x == 0 && FORM == FORM_PLAIN) {
-    mbar_init(bar, 1);
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
     fence_mbar_init();
   }
   __syncthreads();
-  uint32_t phase = 0;
+  uint32_t phase = 0;    // plain form: parity of bars[0]
+  uint32_t phases = 0;   // fast form: bit i = parity of bars[i]
 
   int task_iter = 0;
   for (;;) {
@@ -493,134 +583,161 @@ __global__ void __launch_bounds__(kMaxThreads, 2) semb_search_kernel(KParams P) 
         }
       }
 
-      int64_t ap_pos = ap_begin;
-      while (ap_pos < ap_end) {
-        if (warp == 0) {
-          plan_chunk<METHOD, FORM>(P, pb, ap_pos, ap_end, T_lo, T_hi, meta, srcinfo);
-          if (FORM == FORM_PLAIN) issue_chunk_copies(P, meta, srcinfo, buf, bar);
-        }
-        __syncthreads();
-        const int n = meta->n;
-        if (FORM == FORM_PLAIN) {
-          // wait for the bulk copies of this chunk; give up after kWaitNs
-          bool ok = true;
-          if (!mbar_try_wait(bar, phase)) {
-            const uint64_t t_start = global_ns();
-            while (!mbar_try_wait(bar, phase)) {
-              if (global_ns() - t_start > kWaitNs) {
-                ok = false;
-                break;
+      // compute on a staged chunk (meta, n); the fast form then folds the chunk's
+      // energy into the Kahan totals
+      auto compute_chunk = [&](const ChunkMeta* meta, const int n) {
+          for (int e = 0; e < n; ++e) {
+            const float4 g = meta->geo[e];
+            const int soff = __float_as_int(g.w);
+            if (FORM == FORM_PLAIN) {
+#pragma unroll
+              for (int r = 0; r < RC; ++r) {
+                float t;
+                if (METHOD == METHOD_CMP) {
+                  t = __fmul_rn(__fsqrt_rn(__fadd_rn(T2sec, __fmul_rn(cc[r], g.z))), P.idt);
+                } else {
+                  t = __fadd_rn(Tsec, __fmul_rn(ca[r], g.x));
+                  t = __fadd_rn(__fadd_rn(__fmul_rn(t, t), __fmul_rn(cb[r], g.y)), __fmul_rn(cc[r], g.z));
+                  t = (t < 0.0f) ? -1.0f : __fsqrt_rn(t);
+                  t = __fmul_rn(t, P.idt);
+                }
+                const bool ok = (t >= tau_lo) && (t < tau_hi);
+                const float y = __fadd_rz(t, 8388608.0f);
+                const int it = __float_as_int(y) - 0x4B000000;
+                const float x = ok ? __fsub_rn(t, __fsub_rn(y, 8388608.0f)) : 0.0f;
+                const unsigned idx = min(ok ? (unsigned)(soff + it - P.tau) : (unsigned)P.cap, (unsigned)P.cap);
+                const float* s = buf + idx;
+                float s1 = s[0];
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                  const float s0 = s1;
+                  s1 = s[j + 1];
+                  const float v = __fadd_rn(__fmul_rn(__fsub_rn(s1, s0), x), s0);
+                  pa[r].num[j] = __fadd_rn(pa[r].num[j], v);
+                  pa[r].den = __fadd_rn(pa[r].den, __fmul_rn(v, v));
+                  pa[r].lin = __fadd_rn(pa[r].lin, v);
+                }
+                pa[r].M += ok ? 1 : 0;
+              }
+            } else {
+              // t2 in samples^2 for item r on this trace
+              auto t2_of = [&](int r) {
+                if (METHOD == METHOD_CMP) return fmaf(cc[r], g.z, T2smp);
+                const float u = fmaf(ca[r], g.x, Tsmp);
+                return fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
+              };
+              auto accumulate = [&](int r, uint32_t a, float x) {
+                float sv[W + 1];
+                load_window<W>(a, sv);
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                  const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
+                  fa[r].num[j] += v;
+                  fa[r].den_c = fmaf(v, v, fa[r].den_c);
+                }
+              };
+              if (meta->inrange[e]) {
+                // every item in range: address = bits(t + 2^23) * 16 + base (mod 2^32),
+                // clamped to the buffer as a guard
+                const uint32_t base = bufq_addr + 16u * (uint32_t)(soff - P.tau) - 16u * 0x4B000000u;
+                const uint32_t top = bufq_addr + 16u * (uint32_t)P.cap;
+#pragma unroll
+                for (int r = 0; r < RC; ++r) {
+                  const float t = sqrt_fast(t2_of(r));
+                  const float y = __fadd_rz(t, 8388608.0f);
+                  accumulate(r, min(__float_as_uint(y) * 16u + base, top), t - (y - 8388608.0f));
+                }
+              } else {
+#pragma unroll
+                for (int r = 0; r < RC; ++r) {
+                  const float t = sqrt_fast(t2_of(r));   // NaN for t2 < 0: out of range below
+                  const float y = __fadd_rz(t, 8388608.0f);
+                  const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
+                  const bool ok = (unsigned)rel <= span;
+                  const float x = ok ? t - (y - 8388608.0f) : 0.0f;
+                  const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
+                  accumulate(r, bufq_addr + 16u * idx, x);
+                  fa[r].M += ok ? 1 : 0;
+                }
               }
             }
           }
+          if (FORM == FORM_FAST) {
+            // traces flagged in range count for every item
+            int ninr = 0;
+            for (int e = 0; e < n; ++e) ninr += meta->inrange[e];
+#pragma unroll
+            for (int r = 0; r < RC; ++r) fa[r].M += ninr;
+          }
+          if (FORM == FORM_FAST) {
+#pragma unroll
+            for (int r = 0; r < RC; ++r) {
+              // Kahan: fold this chunk's energy into the compensated total
+              const int o = r * kMaxThreads + threadIdx.x;
+              const float hi = kahan_hi[o], lo = kahan_lo[o];
+              const float yv = fa[r].den_c - lo;
+              const float tv = hi + yv;
+              kahan_lo[o] = (tv - hi) - yv;
+              kahan_hi[o] = tv;
+              fa[r].den_c = 0.f;
+            }
+          }
+      };
+
+      if (FORM == FORM_PLAIN) {
+        int64_t ap_pos = ap_begin;
+        while (ap_pos < ap_end) {
+          if (warp == 0) {
+            plan_chunk<METHOD, FORM>(P, pb, ap_pos, ap_end, T_lo, T_hi, meta, srcinfo);
+            issue_chunk_copies(P, meta, srcinfo, buf, bar);
+          }
+          __syncthreads();
+          const int n = meta->n;
+          // wait for the bulk copies of this chunk; give up after kWaitNs
+          const bool ok = wait_bar(bar, phase);
           phase ^= 1u;
           if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) atomicOr(P.status, ST_TIMEOUT);
             return;
           }
-        } else {
-          stage_fast(P, n, srcinfo, bufq);
-          __syncthreads();
+          compute_chunk(meta, n);
+          ap_pos += n;
+          __syncthreads();   // buffer and meta free for the next chunk
         }
-
-        for (int e = 0; e < n; ++e) {
-          const float4 g = meta->geo[e];
-          const int soff = __float_as_int(g.w);
-          if (FORM == FORM_PLAIN) {
-#pragma unroll
-            for (int r = 0; r < RC; ++r) {
-              float t;
-              if (METHOD == METHOD_CMP) {
-                t = __fmul_rn(__fsqrt_rn(__fadd_rn(T2sec, __fmul_rn(cc[r], g.z))), P.idt);
-              } else {
-                t = __fadd_rn(Tsec, __fmul_rn(ca[r], g.x));
-                t = __fadd_rn(__fadd_rn(__fmul_rn(t, t), __fmul_rn(cb[r], g.y)), __fmul_rn(cc[r], g.z));
-                t = (t < 0.0f) ? -1.0f : __fsqrt_rn(t);
-                t = __fmul_rn(t, P.idt);
-              }
-              const bool ok = (t >= tau_lo) && (t < tau_hi);
-              const float y = __fadd_rz(t, 8388608.0f);
-              const int it = __float_as_int(y) - 0x4B000000;
-              const float x = ok ? __fsub_rn(t, __fsub_rn(y, 8388608.0f)) : 0.0f;
-              const unsigned idx = min(ok ? (unsigned)(soff + it - P.tau) : (unsigned)P.cap, (unsigned)P.cap);
-              const float* s = buf + idx;
-              float s1 = s[0];
-#pragma unroll
-              for (int j = 0; j < W; ++j) {
-                const float s0 = s1;
-                s1 = s[j + 1];
-                const float v = __fadd_rn(__fmul_rn(__fsub_rn(s1, s0), x), s0);
-                pa[r].num[j] = __fadd_rn(pa[r].num[j], v);
-                pa[r].den = __fadd_rn(pa[r].den, __fmul_rn(v, v));
-                pa[r].lin = __fadd_rn(pa[r].lin, v);
-              }
-              pa[r].M += ok ? 1 : 0;
-            }
-          } else {
-            // t2 in samples^2 for item r on this trace
-            auto t2_of = [&](int r) {
-              if (METHOD == METHOD_CMP) return fmaf(cc[r], g.z, T2smp);
-              const float u = fmaf(ca[r], g.x, Tsmp);
-              return fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
-            };
-            auto accumulate = [&](int r, uint32_t a, float x) {
-              float sv[W + 1];
-              load_window<W>(a, sv);
-#pragma unroll
-              for (int j = 0; j < W; ++j) {
-                const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
-                fa[r].num[j] += v;
-                fa[r].den_c = fmaf(v, v, fa[r].den_c);
-              }
-            };
-            if (meta->inrange[e]) {
-              // every item in range: address = bits(t + 2^23) * 16 + base (mod 2^32),
-              // clamped to the buffer as a guard
-              const uint32_t base = bufq_addr + 16u * (uint32_t)(soff - P.tau) - 16u * 0x4B000000u;
-              const uint32_t top = bufq_addr + 16u * (uint32_t)P.cap;
-#pragma unroll
-              for (int r = 0; r < RC; ++r) {
-                const float t = sqrt_fast(t2_of(r));
-                const float y = __fadd_rz(t, 8388608.0f);
-                accumulate(r, min(__float_as_uint(y) * 16u + base, top), t - (y - 8388608.0f));
-              }
-            } else {
-#pragma unroll
-              for (int r = 0; r < RC; ++r) {
-                const float t = sqrt_fast(t2_of(r));   // NaN for t2 < 0: out of range below
-                const float y = __fadd_rz(t, 8388608.0f);
-                const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
-                const bool ok = (unsigned)rel <= span;
-                const float x = ok ? t - (y - 8388608.0f) : 0.0f;
-                const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
-                accumulate(r, bufq_addr + 16u * idx, x);
-                fa[r].M += ok ? 1 : 0;
-              }
+      } else {
+        // software pipeline: while all warps compute chunk c from the quad buffer,
+        // the raw windows of chunk c+1 land in the other raw buffer by TMA
+        int cur = 0;
+        if (warp == 0) {
+          plan_chunk<METHOD, FORM>(P, pb, ap_begin, ap_end, T_lo, T_hi, meta_at(0), srcs);
+          issue_raw(P, meta_at(0), srcs, raw_at(0), &bars[0]);
+        }
+        __syncthreads();
+        int64_t ap_pos = ap_begin;
+        while (ap_pos < ap_end) {
+          ChunkMeta* mc = meta_at(cur);
+          const int n = mc->n;
+          const bool ok = wait_bar(bars + cur, (phases >> cur) & 1u);
+          phases ^= 1u << cur;
+          if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicOr(P.status, ST_TIMEOUT);
+            return;
+          }
+          convert_chunk(P, mc, srcs + cur * kMaxChunk, raw_at(cur), bufq);
+          __syncthreads();   // quads ready; raws[cur] free
+          const int64_t next = ap_pos + n;
+          if (warp == 0) {
+            ChunkMeta* mn = meta_at(cur ^ 1);
+            if (next < ap_end) {
+              plan_chunk<METHOD, FORM>(P, pb, next, ap_end, T_lo, T_hi, mn, srcs + (cur ^ 1) * kMaxChunk);
+              issue_raw(P, mn, srcs + (cur ^ 1) * kMaxChunk, raw_at(cur ^ 1), bars + (cur ^ 1));
             }
           }
+          compute_chunk(mc, n);
+          __syncthreads();   // quad buffer free; the next chunk's metadata visible
+          ap_pos = next;
+          cur ^= 1;
         }
-        if (FORM == FORM_FAST) {
-          // traces flagged in range count for every item
-          int ninr = 0;
-          for (int e = 0; e < n; ++e) ninr += meta->inrange[e];
-#pragma unroll
-          for (int r = 0; r < RC; ++r) fa[r].M += ninr;
-        }
-        if (FORM == FORM_FAST) {
-#pragma unroll
-          for (int r = 0; r < RC; ++r) {
-            // Kahan: fold this chunk's energy into the compensated total
-            const int o = r * kMaxThreads + threadIdx.x;
-            const float hi = kahan_hi[o], lo = kahan_lo[o];
-            const float yv = fa[r].den_c - lo;
-            const float tv = hi + yv;
-            kahan_lo[o] = (tv - hi) - yv;
-            kahan_hi[o] = tv;
-            fa[r].den_c = 0.f;
-          }
-        }
-        ap_pos += n;
-        __syncthreads();   // buffer and meta free for the next chunk
       }
 
       // finalize the pass's items and fold them into this lane's pick
