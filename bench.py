@@ -265,6 +265,7 @@ def run_ours(args, rank, world, dist):
     storage = {"f16": semb.STORE_F16, "bf16": semb.STORE_BF16, "f32": semb.STORE_F32}[args.storage]
     plan = semb.Plan(semb.params(method, mode=semb.BATCHED, storage=storage, **s.params), device=dev)
     plan.upload(arrays.view())
+    tune = plan.autotune() if args.tune else None
     st0 = plan.stats()
     nap = int(round(st0["trace_evals"] / (st0["ns"] * st0["ncand"])))
     # per-kernel split (search vs re-pick) from direct launches
@@ -368,7 +369,9 @@ def run_ours(args, rank, world, dist):
                        "graph": bool(args.graph)},
             "plain_f32": res["plain"], "batched": res["batched"],
             "speedup_batched_vs_plain": res["plain"]["ms"] / (total_ms / args.steps),
-            "roofline": roof, "clocks": clocks, "gpu_launches": int(st["kernel_launches"]) * args.steps}
+            "roofline": roof, "clocks": clocks, "gpu_launches": int(st["kernel_launches"]) * args.steps,
+            "autotune": {"variant": st["variant"], "sample_ms": tune[1] if tune else None,
+                         "ctas_per_sm": st["ctas_per_sm"]}}
     for k in ("store_bf16", "store_f32"):
         if k in res:
             line[k] = res[k]
@@ -396,6 +399,7 @@ def main():
     ap.add_argument("--ncdp", type=int, default=None)
     ap.add_argument("--storage", choices=["f16", "bf16", "f32"], default="f16")
     ap.add_argument("--graph", type=int, default=1)
+    ap.add_argument("--tune", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -85,7 +85,7 @@ typedef struct semb_params {
 } semb_params;
 
 /* Fill `p` with the defaults for `method` (grid fields zero, batched FP16 with
- * near-tie re-pick at gap 2e-3).  Replaces nothing in the reference. */
+ * near-tie re-pick at gap 3e-4).  Replaces nothing in the reference. */
 void semb_params_init(semb_params* p, int32_t method);
 
 /* A linearized gather: what su_gather::linearize hands to the search
@@ -193,9 +193,18 @@ typedef struct semb_stats {
   int32_t grid_ctas;      /* CTAs of the main search launch */
   int32_t ctas_per_sm;    /* resident CTAs per SM of the main search kernel */
   int32_t sms;
+  int32_t variant;        /* search-kernel variant in use (see semb_plan_autotune) */
 } semb_stats;
 
 int semb_plan_stats(const semb_plan* plan, semb_stats* out);
+
+/* Time each variant of the search kernel available for this plan's window
+ * (candidates per thread x resident CTAs per SM) on a strided sample of the
+ * plan's own work queue and keep the fastest for later runs.  *chosen gets the
+ * variant, ms_of_variant[0..2] (optional) the sample times (-1: no such variant).
+ * No counterpart in the reference, which has one fixed launch shape
+ * (CRS/CUDA/src/main.cu:45-51, 439). */
+int semb_plan_autotune(semb_plan* plan, int32_t* chosen, double* ms_of_variant);
 
 /* Capture the search (work-queue reset + kernels) in a CUDA graph and replay it on
  * later semb_plan_run calls (batched form).  on = 0 goes back to direct launches. */

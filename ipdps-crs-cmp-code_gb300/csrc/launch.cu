@@ -7,29 +7,34 @@
 
 namespace semb {
 
-SearchEntry search_entry_cmp_plain(int w);
-SearchEntry search_entry_cmp_fast(int w);
-SearchEntry search_entry_crs_plain(int w);
-SearchEntry search_entry_crs_fast(int w);
+SearchEntry search_entry_cmp_plain(int w, int variant);
+SearchEntry search_entry_cmp_fast(int w, int variant);
+SearchEntry search_entry_crs_plain(int w, int variant);
+SearchEntry search_entry_crs_fast(int w, int variant);
 
-static SearchEntry lookup(int method, int form, int w) {
-  if (method == METHOD_CMP) return form == FORM_PLAIN ? search_entry_cmp_plain(w) : search_entry_cmp_fast(w);
-  return form == FORM_PLAIN ? search_entry_crs_plain(w) : search_entry_crs_fast(w);
+static SearchEntry lookup(int method, int form, int w, int v) {
+  if (method == METHOD_CMP) return form == FORM_PLAIN ? search_entry_cmp_plain(w, v) : search_entry_cmp_fast(w, v);
+  return form == FORM_PLAIN ? search_entry_crs_plain(w, v) : search_entry_crs_fast(w, v);
 }
 
-int search_rc(int method, int form, int w) { return lookup(method, form, w).rc; }
+int search_variant(int method, int form, int w, int v, int* rc, int* minb) {
+  SearchEntry e = lookup(method, form, w, v);
+  *rc = e.rc;
+  *minb = e.minb;
+  return e.fn != nullptr;
+}
 
-int search_occupancy(int method, int form, int w, int nwarps, size_t smem, int* ctas_per_sm) {
-  SearchEntry e = lookup(method, form, w);
+int search_occupancy(int method, int form, int w, int v, int nwarps, size_t smem, int* ctas_per_sm) {
+  SearchEntry e = lookup(method, form, w, v);
   if (!e.fn) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", w);
   SEMB_CUDA(cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SEMB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas_per_sm, e.fn, nwarps * 32, smem));
   return SEMB_OK;
 }
 
-int launch_search(int method, int form, int w, const KParams& P, int nwarps, int grid, size_t smem,
+int launch_search(int method, int form, int w, int v, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st) {
-  SearchEntry e = lookup(method, form, w);
+  SearchEntry e = lookup(method, form, w, v);
   if (!e.fn) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", w);
   void* args[] = {const_cast<KParams*>(&P)};
   SEMB_CUDA(cudaLaunchKernel(e.fn, dim3(grid), dim3(nwarps * 32), args, smem, st));

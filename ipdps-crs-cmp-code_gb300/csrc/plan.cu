@@ -24,10 +24,10 @@
 namespace semb {
 
 // Launchers of the search kernel instantiations (kernels_*.cu).
-int launch_search(int method, int form, int w, const KParams& P, int nwarps, int grid, size_t smem,
+int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
-int search_rc(int method, int form, int w);
-int search_occupancy(int method, int form, int w, int nwarps, size_t smem, int* ctas_per_sm);
+int search_variant(int method, int form, int w, int variant, int* rc, int* minb);
+int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);
 
@@ -54,6 +54,11 @@ struct semb_plan {
   int grid = 0, ctas_per_sm = 0;
   int64_t n_nbr = 0;
   float cand0_a = 0.f, cand0_b = 0.f, cand0_c = 0.f;
+  int variant = 0, minb = 2;
+  // candidate grid kept on the host for re-configuration
+  std::vector<float> ga, gb, gc;
+  std::vector<double> g64;
+  std::vector<int> order;
 
   // device buffers
   float* d_samples = nullptr;
@@ -223,6 +228,98 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
       abc[3 * (size_t)i + 2] = c0 + pc;
     }
   }
+}
+
+// Launch configuration of search-kernel variant v: candidates per pass (warps x
+// RC, warps chosen to waste the least padding), the search-order candidate
+// table padded to whole passes, per-pass parameter bounds, the staging capacity
+// (as large as the variant's resident CTAs per SM allow, never less than one
+// whole trace), shared memory, occupancy and grid.
+int configure_variant(semb_plan* pl, int v) {
+  const semb_params& p = pl->p;
+  const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
+  int rc = 0, minb = 0;
+  if (!search_variant(p.method, form, pl->w, v, &rc, &minb))
+    return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
+  const int ncand = pl->ncand;
+  int best_nw = 8, best_tot = INT32_MAX;
+  for (int nw = 8; nw >= 4; --nw) {
+    const int per = nw * rc;
+    const int tot = ((ncand + per - 1) / per) * per;
+    if (tot < best_tot) {
+      best_tot = tot;
+      best_nw = nw;
+    }
+  }
+  const int cpp = best_nw * rc;
+  const int npass = (ncand + cpp - 1) / cpp;
+  const int npad = npass * cpp;
+  std::vector<float4> cand(npad);
+  std::vector<float> bounds((size_t)npass * 8, 0.f);
+  const double s1 = pl->idt64, s2 = pl->idt64 * pl->idt64;
+  for (int k = 0; k < npad; ++k) {
+    const int gi = pl->order[std::min(k, ncand - 1)];
+    float4 c;
+    if (form == FORM_PLAIN) {
+      c = make_float4(pl->ga[gi], pl->gb[gi], pl->gc[gi], 0.f);
+    } else {
+      c = make_float4((float)(pl->g64[3 * (size_t)gi] * s1), (float)(pl->g64[3 * (size_t)gi + 1] * s2),
+                      (float)(pl->g64[3 * (size_t)gi + 2] * s2), 0.f);
+    }
+    int32_t gbits = gi;
+    std::memcpy(&c.w, &gbits, 4);
+    cand[k] = c;
+    float* bp = &bounds[(size_t)(k / cpp) * 8];
+    if (k % cpp == 0) {
+      bp[0] = bp[1] = pl->ga[gi];
+      bp[2] = bp[3] = pl->gb[gi];
+      bp[4] = bp[5] = pl->gc[gi];
+    } else {
+      bp[0] = std::min(bp[0], pl->ga[gi]);
+      bp[1] = std::max(bp[1], pl->ga[gi]);
+      bp[2] = std::min(bp[2], pl->gb[gi]);
+      bp[3] = std::max(bp[3], pl->gb[gi]);
+      bp[4] = std::min(bp[4], pl->gc[gi]);
+      bp[5] = std::max(bp[5], pl->gc[gi]);
+    }
+  }
+  dev_free(pl->d_cand);
+  dev_free(pl->d_pass_bounds);
+  SEMB_TRY(dev_alloc(&pl->d_cand, npad));
+  SEMB_TRY(dev_alloc(&pl->d_pass_bounds, bounds.size()));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_cand, cand.data(), npad * sizeof(float4), cudaMemcpyHostToDevice, pl->stream));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_pass_bounds, bounds.data(), bounds.size() * 4, cudaMemcpyHostToDevice,
+                            pl->stream));
+
+  const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
+  const size_t budget = (227 * 1024) / minb - 1024;
+  int cap = form == FORM_PLAIN ? 32768 : 8192;
+  while (cap > 64 && smem_layout(form, rc, cap, store).total > budget) cap -= 64;
+  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
+  const size_t smem = smem_layout(form, rc, cap, store).total;
+  if (smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", pl->ns);
+  int occ = 0;
+  SEMB_TRY(search_occupancy(p.method, form, pl->w, v, best_nw, smem, &occ));
+  if (occ <= 0) return fail(SEMB_E_CUDA, "search kernel cannot be resident with %zu bytes", smem);
+  SEMB_CUDA(cudaStreamSynchronize(pl->stream));
+  pl->variant = v;
+  pl->rc = rc;
+  pl->minb = minb;
+  pl->nwarps = best_nw;
+  pl->cpp = cpp;
+  pl->npass = npass;
+  pl->cap = cap;
+  pl->smem = smem;
+  pl->ctas_per_sm = occ;
+  pl->grid = form == FORM_PLAIN ? pl->ntasks : std::min(pl->ntasks, pl->sms * occ);
+  pl->stats.grid_ctas = pl->grid;
+  pl->stats.ctas_per_sm = occ;
+  pl->stats.variant = v;
+  if (pl->graph) {
+    cudaGraphExecDestroy(pl->graph);
+    pl->graph = nullptr;
+  }
+  return SEMB_OK;
 }
 
 }  // namespace
@@ -438,79 +535,28 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
     SEMB_CUDA(cudaGetLastError());
   }
 
-  // candidate grid, search order and passes
-  std::vector<float> ga, gb, gc;
-  grid_f32(p, ga, gb, gc);
-  std::vector<double> g64;
-  grid_f64(p, g64);
-  const int ncand = (int)gc.size();
+  // candidate grid and search order
+  grid_f32(p, pl->ga, pl->gb, pl->gc);
+  grid_f64(p, pl->g64);
+  const int ncand = (int)pl->gc.size();
   pl->ncand = ncand;
-  pl->cand0_a = ga[0];
-  pl->cand0_b = gb[0];
-  pl->cand0_c = gc[0];
-  std::vector<int> order(ncand);
+  pl->cand0_a = pl->ga[0];
+  pl->cand0_b = pl->gb[0];
+  pl->cand0_c = pl->gc[0];
+  pl->order.resize(ncand);
   if (p.method == SEMB_CMP) {
-    std::iota(order.begin(), order.end(), 0);
+    std::iota(pl->order.begin(), pl->order.end(), 0);
   } else {
     // C outermost, then A, then B: a pass spans few C values, which dominate the
     // spread of traveltimes, so its staged windows stay narrow.
     int q = 0;
     for (int ic = 0; ic < p.nc; ++ic)
       for (int ia = 0; ia < p.na; ++ia)
-        for (int ib = 0; ib < p.nb; ++ib) order[q++] = ia * p.nb * p.nc + ib * p.nc + ic;
+        for (int ib = 0; ib < p.nb; ++ib) pl->order[q++] = ia * p.nb * p.nc + ib * p.nc + ic;
   }
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  const int rc = search_rc(p.method, form, pl->w);
-  if (rc <= 0) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", pl->w);
-  int best_nw = 8, best_tot = INT32_MAX;
-  for (int nw = 8; nw >= 4; --nw) {
-    const int per = nw * rc;
-    const int tot = ((ncand + per - 1) / per) * per;
-    if (tot < best_tot) {
-      best_tot = tot;
-      best_nw = nw;
-    }
-  }
-  pl->nwarps = best_nw;
-  pl->rc = rc;
-  pl->cpp = best_nw * rc;
-  pl->npass = (ncand + pl->cpp - 1) / pl->cpp;
-  const int npad = pl->npass * pl->cpp;
-  std::vector<float4> cand(npad);
-  std::vector<float> bounds((size_t)pl->npass * 8, 0.f);
-  const double s1 = pl->idt64, s2 = pl->idt64 * pl->idt64;
-  for (int k = 0; k < npad; ++k) {
-    const int gi = order[std::min(k, ncand - 1)];
-    float4 v;
-    if (form == FORM_PLAIN) {
-      v = make_float4(ga[gi], gb[gi], gc[gi], 0.f);
-    } else {
-      v = make_float4((float)(g64[3 * (size_t)gi] * s1), (float)(g64[3 * (size_t)gi + 1] * s2),
-                      (float)(g64[3 * (size_t)gi + 2] * s2), 0.f);
-    }
-    int32_t gbits = gi;
-    std::memcpy(&v.w, &gbits, 4);
-    cand[k] = v;
-    float* bp = &bounds[(size_t)(k / pl->cpp) * 8];
-    if (k % pl->cpp == 0) {
-      bp[0] = bp[1] = ga[gi];
-      bp[2] = bp[3] = gb[gi];
-      bp[4] = bp[5] = gc[gi];
-    } else {
-      bp[0] = std::min(bp[0], ga[gi]);
-      bp[1] = std::max(bp[1], ga[gi]);
-      bp[2] = std::min(bp[2], gb[gi]);
-      bp[3] = std::max(bp[3], gb[gi]);
-      bp[4] = std::min(bp[4], gc[gi]);
-      bp[5] = std::max(bp[5], gc[gi]);
-    }
-  }
-  SEMB_TRY(dev_alloc(&pl->d_cand, npad));
-  SEMB_TRY(dev_alloc(&pl->d_pass_bounds, bounds.size()));
-  SEMB_TRY(dev_alloc(&pl->d_cand64, g64.size()));
-  SEMB_CUDA(cudaMemcpyAsync(pl->d_cand, cand.data(), npad * sizeof(float4), cudaMemcpyHostToDevice, st));
-  SEMB_CUDA(cudaMemcpyAsync(pl->d_pass_bounds, bounds.data(), bounds.size() * 4, cudaMemcpyHostToDevice, st));
-  SEMB_CUDA(cudaMemcpyAsync(pl->d_cand64, g64.data(), g64.size() * 8, cudaMemcpyHostToDevice, st));
+  SEMB_TRY(dev_alloc(&pl->d_cand64, pl->g64.size()));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_cand64, pl->g64.data(), pl->g64.size() * 8, cudaMemcpyHostToDevice, st));
 
   // work queue: (cdp, t0 block), largest aperture first (longest-processing-time order)
   const int nblk = (g->ns + kTB - 1) / kTB;
@@ -542,19 +588,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
     SEMB_TRY(dev_alloc(&pl->d_top_stk, nout * kTopK));
   }
 
-  // staging capacity: as large as two resident CTAs per SM allow (about 113 KB of
-  // shared memory each), and never less than one whole trace
-  const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
-  const size_t budget = 113 * 1024;
-  int cap = form == FORM_PLAIN ? 32768 : 8192;
-  while (cap > 64 && smem_layout(form, rc, cap, store).total > budget) cap -= 64;
-  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
-  pl->cap = cap;
-  pl->smem = smem_layout(form, rc, cap, store).total;
-  if (pl->smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", g->ns);
-  SEMB_TRY(search_occupancy(p.method, form, pl->w, pl->nwarps, pl->smem, &pl->ctas_per_sm));
-  if (pl->ctas_per_sm <= 0) return fail(SEMB_E_CUDA, "search kernel cannot be resident with %zu bytes", pl->smem);
-  pl->grid = form == FORM_PLAIN ? pl->ntasks : std::min(pl->ntasks, pl->sms * pl->ctas_per_sm);
+  SEMB_TRY(configure_variant(pl, 0));
   cudaEventRecord(pl->ev[5], st);
   SEMB_CUDA(cudaStreamSynchronize(st));
   float ms = 0.f;
@@ -572,6 +606,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   pl->stats.trace_evals = pl->nap * (int64_t)pl->ns * pl->ncand;
   pl->stats.grid_ctas = pl->grid;
   pl->stats.ctas_per_sm = pl->ctas_per_sm;
+  pl->stats.variant = pl->variant;
   pl->stats.sms = pl->sms;
   pl->uploaded = true;
   return SEMB_OK;
@@ -641,7 +676,7 @@ int enqueue_run(semb_plan* pl, bool timed) {
   }
   if (form == FORM_FAST) SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st));
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[1], st));
-  SEMB_TRY(launch_search(p.method, form, pl->w, P, pl->nwarps, pl->grid, pl->smem, st));
+  SEMB_TRY(launch_search(p.method, form, pl->w, pl->variant, P, pl->nwarps, pl->grid, pl->smem, st));
   ++launches;
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
   if (form == FORM_FAST) {
@@ -761,6 +796,59 @@ int semb_plan_neighbours(semb_plan* pl, int32_t* off, int32_t* list, int64_t* n_
     for (size_t i = 0; i < o.size(); ++i) off[i] = (int32_t)o[i];
   }
   if (list) SEMB_CUDA(cudaMemcpy(list, pl->d_nbr, (size_t)pl->n_nbr * 4, cudaMemcpyDeviceToHost));
+  return SEMB_OK;
+}
+
+int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_autotune before semb_plan_upload");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  const semb_params& p = pl->p;
+  const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
+  cudaStream_t st = pl->stream;
+  // a strided sample of the (aperture-sorted) task list: big and small apertures
+  const int S = std::min(pl->ntasks, std::max(1, pl->sms * 12));
+  std::vector<int2> all(pl->ntasks), sample(S);
+  SEMB_CUDA(cudaMemcpy(all.data(), pl->d_tasks, all.size() * sizeof(int2), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < S; ++i) sample[i] = all[(int64_t)i * pl->ntasks / S];
+  int2* d_sample = nullptr;
+  SEMB_TRY(dev_alloc(&d_sample, S));
+  struct Free {
+    int2* p;
+    ~Free() { cudaFree(p); }
+  } guard{d_sample};
+  SEMB_CUDA(cudaMemcpy(d_sample, sample.data(), S * sizeof(int2), cudaMemcpyHostToDevice));
+  int best = -1;
+  double best_ms = 1e300;
+  for (int v = 0; v < 3; ++v) {
+    int rc = 0, minb = 0;
+    if (ms_of_variant) ms_of_variant[v] = -1.0;
+    if (!search_variant(p.method, form, pl->w, v, &rc, &minb)) continue;
+    SEMB_TRY(configure_variant(pl, v));
+    KParams P = make_kparams(pl);
+    P.tasks = d_sample;
+    P.ntasks = S;
+    const int grid = form == FORM_PLAIN ? S : std::min(S, pl->sms * pl->ctas_per_sm);
+    float ms = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st));
+      SEMB_CUDA(cudaEventRecord(pl->ev[4], st));
+      SEMB_TRY(launch_search(p.method, form, pl->w, v, P, pl->nwarps, grid, pl->smem, st));
+      SEMB_CUDA(cudaEventRecord(pl->ev[5], st));
+      SEMB_CUDA(cudaStreamSynchronize(st));
+      float t = 0.f;
+      SEMB_CUDA(cudaEventElapsedTime(&t, pl->ev[4], pl->ev[5]));
+      if (rep > 0) ms = std::min(ms, t);   // the first launch is a warm-up
+    }
+    if (ms_of_variant) ms_of_variant[v] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  if (best < 0) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", pl->w);
+  SEMB_TRY(configure_variant(pl, best));
+  if (chosen) *chosen = best;
   return SEMB_OK;
 }
 

@@ -316,6 +316,11 @@ static __global__ void k_repick(RepickParams R) {
   const bool none = !(ts[0] > 0.f) || ti[0] < 0;
   const bool near_tie = ti[1] >= 0 && ts[1] > 0.f && (ts[0] - ts[1]) < R.gap;
   const bool redo = !none && (R.mode == 2 || (R.mode == 1 && near_tie));
+  // candidates that can still win: the best and those within `gap` of it (all
+  // four in mode 2); the others keep their single-precision rank below the best
+#pragma unroll
+  for (int q = 1; q < kTopK; ++q)
+    if (ti[q] >= 0 && !(R.mode == 2 || (ts[0] - ts[q]) < R.gap)) ti[q] = -1;
   int out_i = ti[0];
   float out_s = ts[0], out_k = tk[0];
   if (redo) {
@@ -344,6 +349,7 @@ static __global__ void k_repick(RepickParams R) {
       const float* row = R.samples + (int64_t)R.ap_tr[e] * R.pitch;
 #pragma unroll
       for (int q = 0; q < kTopK; ++q) {
+        if (ti[q] < 0) continue;
         double t;
         if (R.method == METHOD_CMP) {
           t = sqrt(T * T + pc[q] * g.h) * R.idt;

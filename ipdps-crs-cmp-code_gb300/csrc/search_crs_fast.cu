@@ -3,5 +3,5 @@
 #include "search_inst.cuh"
 
 namespace semb {
-SearchEntry search_entry_crs_fast(int w) { return search_entry<METHOD_CRS, FORM_FAST>(w); }
+SearchEntry search_entry_crs_fast(int w, int variant) { return search_entry<METHOD_CRS, FORM_FAST>(w, variant); }
 }  // namespace semb

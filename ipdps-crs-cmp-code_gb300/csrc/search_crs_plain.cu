@@ -3,5 +3,5 @@
 #include "search_inst.cuh"
 
 namespace semb {
-SearchEntry search_entry_crs_plain(int w) { return search_entry<METHOD_CRS, FORM_PLAIN>(w); }
+SearchEntry search_entry_crs_plain(int w, int variant) { return search_entry<METHOD_CRS, FORM_PLAIN>(w, variant); }
 }  // namespace semb

@@ -1,7 +1,12 @@
-// Instantiation table of the search kernel for one (method, form): one kernel per
-// window width w = 2*tau+1, with the number of candidates per thread (RC) chosen
-// so that the per-item register state fits two 256-thread CTAs per SM without
-// spilling (checked with -Xptxas -v).
+// Instantiation table of the search kernel for one (method, form).  For each
+// window width w = 2*tau+1 there are one or more variants (RC candidates per
+// thread, MINB resident CTAs per SM): more items per thread give more
+// instruction-level parallelism and amortize per-trace work, more CTAs per SM
+// give the scheduler more warps to hide barrier and load latency.  The plan's
+// autotuner times the variants of its window on a sample of its own tasks and
+// keeps the fastest; variant 0 is the default.  RC values keep the per-item
+// register state within 65536 / (256 * MINB) registers without spilling
+// (checked with -Xptxas -v).
 #pragma once
 
 #include "common.h"
@@ -12,36 +17,67 @@ namespace semb {
 struct SearchEntry {
   const void* fn;
   int rc;
+  int minb;
 };
 
-template <int METHOD, int FORM, int W>
-constexpr int rc_for() {
-  if (FORM == FORM_PLAIN) return W <= 5 ? 8 : W == 7 ? 6 : W <= 11 ? 4 : W == 13 ? 3 : 2;
-  if (METHOD == METHOD_CRS) return W == 1 ? 8 : 6;
-  return W <= 5 ? 8 : W <= 9 ? 4 : W <= 13 ? 3 : 2;
+constexpr int kMaxVariants = 3;
+
+template <int METHOD, int FORM, int W, int RC, int MINB>
+SearchEntry entry() {
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB>, RC, MINB};
 }
 
-template <int METHOD, int FORM, int W>
-SearchEntry entry() {
-  constexpr int RC = rc_for<METHOD, FORM, W>();
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC>, RC};
+// Plain form: one variant per window.
+template <int METHOD, int W>
+SearchEntry plain_entry() {
+  constexpr int RC = W <= 5 ? 8 : W == 7 ? 6 : W <= 11 ? 4 : W == 13 ? 3 : 2;
+  return entry<METHOD, FORM_PLAIN, W, RC, 2>();
 }
 
 template <int METHOD, int FORM>
-SearchEntry search_entry(int w) {
-  switch (w) {
-    case 1: return entry<METHOD, FORM, 1>();
-    case 3: return entry<METHOD, FORM, 3>();
-    case 5: return entry<METHOD, FORM, 5>();
+SearchEntry search_entry(int w, int variant) {
+  if (FORM == FORM_PLAIN) {
+    if (variant != 0) return {nullptr, 0, 0};
+    switch (w) {
+      case 1: return plain_entry<METHOD, 1>();
+      case 3: return plain_entry<METHOD, 3>();
+      case 5: return plain_entry<METHOD, 5>();
 #if SEMB_WIDE_WINDOWS
-    case 7: return entry<METHOD, FORM, 7>();
-    case 9: return entry<METHOD, FORM, 9>();
-    case 11: return entry<METHOD, FORM, 11>();
-    case 13: return entry<METHOD, FORM, 13>();
-    case 15: return entry<METHOD, FORM, 15>();
+      case 7: return plain_entry<METHOD, 7>();
+      case 9: return plain_entry<METHOD, 9>();
+      case 11: return plain_entry<METHOD, 11>();
+      case 13: return plain_entry<METHOD, 13>();
+      case 15: return plain_entry<METHOD, 15>();
 #endif
-    default: return {nullptr, 0};
+      default: return {nullptr, 0, 0};
+    }
   }
+  // fast form
+  switch (w) {
+    case 1:
+      if (variant == 0) return entry<METHOD, FORM, 1, 8, 2>();
+      if (variant == 1) return entry<METHOD, FORM, 1, 4, 3>();
+      break;
+    case 3:
+      if (variant == 0) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
+      if (variant == 1) return entry<METHOD, FORM, 3, 4, 3>();
+      if (variant == 2) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 6 : 8), 2>();
+      break;
+    case 5:
+      if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
+      if (variant == 1) return entry<METHOD, FORM, 5, 4, 3>();
+      if (variant == 2) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 6 : 4), 2>();
+      break;
+#if SEMB_WIDE_WINDOWS
+    case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;
+    case 9: if (variant == 0) return entry<METHOD, FORM, 9, 4, 2>(); break;
+    case 11: if (variant == 0) return entry<METHOD, FORM, 11, 3, 2>(); break;
+    case 13: if (variant == 0) return entry<METHOD, FORM, 13, 3, 2>(); break;
+    case 15: if (variant == 0) return entry<METHOD, FORM, 15, 2, 2>(); break;
+#endif
+    default: break;
+  }
+  return {nullptr, 0, 0};
 }
 
 }  // namespace semb

@@ -461,8 +461,8 @@ __host__ __device__ constexpr size_t kahan_bytes(int form, int rc) {
 // ---------------------------------------------------------------------------
 // The search kernel.
 
-template <int METHOD, int FORM, int W, int RC>
-__global__ void __launch_bounds__(kMaxThreads, 2) semb_search_kernel(KParams P) {
+template <int METHOD, int FORM, int W, int RC, int MINB>
+__global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);   // [2]

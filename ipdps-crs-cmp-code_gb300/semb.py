@@ -34,7 +34,7 @@ OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODE
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
-    "semb_plan_neighbours", "semb_plan_stats", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
+    "semb_plan_neighbours", "semb_plan_stats", "semb_plan_autotune", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
     "semb_host_free", "semb_probe_fp32", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
 
@@ -67,6 +67,7 @@ class SembStats(C.Structure):
         ("evals", C.c_int64), ("trace_evals", C.c_int64), ("repicked", C.c_int64), ("kernel_launches", C.c_int64),
         ("window", C.c_int32), ("max_aperture", C.c_int32), ("ncdps", C.c_int32), ("ns", C.c_int32),
         ("ncand", C.c_int32), ("grid_ctas", C.c_int32), ("ctas_per_sm", C.c_int32), ("sms", C.c_int32),
+        ("variant", C.c_int32),
     ]
 
     def as_dict(self) -> dict:
@@ -104,6 +105,7 @@ def lib():
         "semb_plan_download": (C.c_int, [P, P, P, P]),
         "semb_plan_neighbours": (C.c_int, [P, P, P, P]),
         "semb_plan_stats": (C.c_int, [P, P]),
+        "semb_plan_autotune": (C.c_int, [P, P, P]),
         "semb_plan_use_graph": (C.c_int, [P, i32]),
         "semb_plan_destroy": (C.c_int, [P]),
         "semb_host_alloc": (C.c_int, [C.c_size_t, P]),
@@ -133,7 +135,7 @@ def _ptr(a: np.ndarray | None):
 
 
 def params(method: int, mode: int = PLAIN_F32, storage: int = STORE_F16, repick: int = REPICK_NEAR_TIES,
-           repick_gap: float = 2e-3, **kw) -> SembParams:
+           repick_gap: float = 3e-4, **kw) -> SembParams:
     """Build semb_params from the reference's flag names (c0, c1, nc, aph, tau, and
     for CRS a0, a1, na, b0, b1, nb, apm, azimuth).  CMP values are rounded to float
     first, as the reference's stof does."""
@@ -276,6 +278,14 @@ class Plan:
         lst = np.zeros(max(1, n.value), np.int32)
         _check(lib().semb_plan_neighbours(self._h, _ptr(off), _ptr(lst), None), "semb_plan_neighbours")
         return off, lst[:n.value]
+
+    def autotune(self):
+        """Pick the fastest search-kernel variant on a sample of this plan's tasks.
+        Returns (chosen variant, [sample ms per variant, -1 when absent])."""
+        v = C.c_int32()
+        ms = (C.c_double * 3)()
+        _check(lib().semb_plan_autotune(self._h, C.byref(v), ms), "semb_plan_autotune")
+        return int(v.value), [float(x) for x in ms]
 
     def stats(self) -> dict:
         s = SembStats()
