@@ -191,7 +191,8 @@ def cmp_survey(seed=0, ncmp=200, fold=60, ns=1000, dt_us=2000, nevents=5, nc=101
     else:
         hofs = [25.0 + 12.5 * np.arange(fold)] * ncmp
     t_end = 0.9 * ns * dt_us * 1e-6
-    ev = _events(rng, ncmp, nevents, (0.3, min(1.8, t_end)), None, None, (CMP_GRID["c0"], CMP_GRID["c1"]))
+    ev = _events(rng, ncmp, nevents, (min(0.3, 0.5 * t_end), min(1.8, t_end)), None, None,
+                 (CMP_GRID["c0"], CMP_GRID["c1"]))
     # C = 4/v^2 with v ~ U[1500, 4500] m/s
     v = rng.uniform(1500.0, 4500.0, size=(ncmp, nevents))
     ev[..., 3] = 4.0 / (v * v)
@@ -255,7 +256,7 @@ def crs_survey(seed=2, ncdp=500, noffsets=48, ns=1000, dt_us=2000, nevents=4, na
     blk_of = np.arange(ncdp) // block
     centre = np.stack([pos[blk_of == b].mean(axis=0) for b in range(nblk)])
     t_end = 0.9 * ns * dt_us * 1e-6
-    ev = _events(rng, nblk, nevents, (0.3, min(1.8, t_end)), (CRS_GRID["a0"], CRS_GRID["a1"]),
+    ev = _events(rng, nblk, nevents, (min(0.3, 0.5 * t_end), min(1.8, t_end)), (CRS_GRID["a0"], CRS_GRID["a1"]),
                  (CRS_GRID["b0"], CRS_GRID["b1"]), (CRS_GRID["c0"], CRS_GRID["c1"]))
     params = dict(CRS_GRID, na=na, nb=nb, nc=nc, aph=aph, apm=apm, tau=tau, azimuth=azimuth)
     s = _build("crs", pos, line_dir, hofs, ev, blk_of, centre, ns, dt_us, seed,
