@@ -176,6 +176,26 @@ int semb_plan_download(semb_plan* plan, int32_t* ctr, float* str, float* stk);
  * su_gather::su_gather (CRS/OpenMP/src/su_gather.cpp:70-87). */
 int semb_plan_neighbours(semb_plan* plan, int32_t* off, int32_t* list, int64_t* n_out);
 
+/* Neighbour lists with no device allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc while they run (device memory owned by
+ * another allocator, allocation-free real-time loops, work recorded into a CUDA
+ * graph).  The caller passes device pointers: the first trace's gx, gy, sx, sy
+ * and scalco of each of ncdps CDPs (inputs) and off[ncdps+1] and list[capacity]
+ * (outputs, the same lists semb_plan_neighbours returns for a plan).  Scratch
+ * lives in one fixed array inside this library, 2.5 MB on every GPU that loads
+ * it, kept until the process exits, so ncdps is limited to 131072 (larger is
+ * SEMB_E_ARG).  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress), so make one call before any stream capture.  The call
+ * enqueues on `stream` (a cudaStream_t, NULL for the legacy default stream) and
+ * synchronizes it to return the list length in *n_list; if that exceeds
+ * capacity the lists are truncated and SEMB_E_ARG is returned.  All calls share
+ * the scratch: calls that overlap on the GPU (other threads, other streams)
+ * race and must be serialized by the caller. */
+int semb_neighbours_noalloc(const int32_t* gx, const int32_t* gy, const int32_t* sx, const int32_t* sy,
+                            const int32_t* scalco, int32_t ncdps, int32_t apm, int32_t* off, int32_t* list,
+                            int64_t capacity, int64_t* n_list, void* stream);
+
 typedef struct semb_stats {
   double ms_search;       /* device time of the last run's semblance kernel(s);
                              0 when the run was a graph replay */

@@ -34,7 +34,7 @@ OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODE
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
-    "semb_plan_neighbours", "semb_plan_stats", "semb_plan_autotune", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
+    "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
     "semb_host_free", "semb_probe_fp32", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
 
@@ -105,6 +105,7 @@ def lib():
         "semb_plan_download": (C.c_int, [P, P, P, P]),
         "semb_plan_neighbours": (C.c_int, [P, P, P, P]),
         "semb_plan_stats": (C.c_int, [P, P]),
+        "semb_neighbours_noalloc": (C.c_int, [P, P, P, P, P, i32, i32, P, P, i64, P, P]),
         "semb_plan_autotune": (C.c_int, [P, P, P]),
         "semb_plan_use_graph": (C.c_int, [P, i32]),
         "semb_plan_destroy": (C.c_int, [P]),
@@ -327,6 +328,19 @@ class PinnedArray:
             self.array = None
             lib().semb_host_free(self._ptr)
             self._ptr = None
+
+
+def neighbours_noalloc(gx_ptr, gy_ptr, sx_ptr, sy_ptr, scalco_ptr, ncdps: int, apm: int, off_ptr, list_ptr,
+                       capacity: int, stream_ptr=None) -> int:
+    """semb_neighbours_noalloc on caller-owned device buffers (raw device pointers
+    as ints).  Returns the list length."""
+    n = C.c_int64()
+    _check(lib().semb_neighbours_noalloc(C.c_void_p(gx_ptr), C.c_void_p(gy_ptr), C.c_void_p(sx_ptr),
+                                         C.c_void_p(sy_ptr), C.c_void_p(scalco_ptr), int(ncdps), int(apm),
+                                         C.c_void_p(off_ptr), C.c_void_p(list_ptr), int(capacity), C.byref(n),
+                                         C.c_void_p(stream_ptr) if stream_ptr else None),
+           "semb_neighbours_noalloc")
+    return int(n.value)
 
 
 def probe_fp32_tflops(device: int = 0) -> float:
