@@ -129,9 +129,10 @@ int semb_survey_from_bytes(const void* su_bytes, int64_t nbytes, int32_t method,
 int semb_survey_view(const semb_survey* s, semb_gather_view* out);
 
 /* Write the reference's output files into out_dir: cmp.{c,coher,stack}.su or
- * crs.{a,b,c,coher,stack}.su, one trace per CDP in the survey's CDP order, each a
- * copy of the CDP's first trace header with offset 0 and sx=gx, sy=gy set to the
- * integer midpoint (CRS/OpenMP/src/main.cpp:331-359).  ctr/str/stk are
+ * crs.{a,b,c,coher,stack}.su, one trace per CDP in the survey's CDP order, each
+ * with a copy of the CDP's first trace header; in the parameter files (c, a, b)
+ * offset is 0 and sx=gx, sy=gy hold the integer midpoint, in the coherence and
+ * stack files the header is unchanged (CRS/OpenMP/src/main.cpp:331-359).  ctr/str/stk are
  * [ncdps * ns] as returned by semb_plan_download. */
 int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t* ctr,
                       const float* str, const float* stk, const char* out_dir);

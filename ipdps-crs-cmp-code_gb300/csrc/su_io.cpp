@@ -275,10 +275,15 @@ int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t*
   }
   // attribute grids exactly as the writer computes them
   std::vector<float> vals((size_t)ns);
-  unsigned char hdr[kHdrSize];
+  unsigned char hdr0[kHdrSize], hdr[kHdrSize];
   bool ok = true;
   for (int i = 0; i < ncdps && ok; ++i) {
-    std::memcpy(hdr, &s->first_hdr[(size_t)i * kHdrSize], kHdrSize);
+    // attribute files (c, or a/b/c): the first trace's header with offset 0 and
+    // source and receiver at the integer midpoint; coherence and stack files: the
+    // first trace's header unchanged (CMP/OpenMP/src/main.cpp:245-251,
+    // CRS/OpenMP/src/main.cpp:332-346)
+    std::memcpy(hdr0, &s->first_hdr[(size_t)i * kHdrSize], kHdrSize);
+    std::memcpy(hdr, hdr0, kHdrSize);
     const int32_t sx0 = rd_i32(hdr, kOffSx), gx0 = rd_i32(hdr, kOffGx);
     const int32_t sy0 = rd_i32(hdr, kOffSy), gy0 = rd_i32(hdr, kOffGy);
     wr_i32(hdr, kOffOffset, 0);
@@ -329,7 +334,8 @@ int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t*
           data = (k == 3 ? str : stk) + (size_t)i * ns;
         }
       }
-      ok = std::fwrite(hdr, 1, kHdrSize, f[k]) == (size_t)kHdrSize &&
+      const bool attribute = k < nout - 2;
+      ok = std::fwrite(attribute ? hdr : hdr0, 1, kHdrSize, f[k]) == (size_t)kHdrSize &&
            std::fwrite(data, sizeof(float), (size_t)ns, f[k]) == (size_t)ns;
     }
   }

@@ -226,7 +226,7 @@ def crs_survey(seed=2, ncdp=500, noffsets=48, ns=1000, dt_us=2000, nevents=4, na
         target = np.exp(rng.uniform(math.log(lo), math.log(hi), size=nblk))
         spacing_cdp = np.empty(ncdp)
         folds = np.empty(ncdp, dtype=int)
-        hmax_blk = rng.uniform(600.0, float(aph), size=nblk)
+        hmax_blk = rng.uniform(min(600.0, 0.5 * aph), float(aph), size=nblk)
         for b in range(nblk):
             n = target[b]
             # spacing -> neighbours within apm (both sides + self); keep clear of the apm boundary
