@@ -244,6 +244,13 @@ int semb_host_free(void* p);
  * search kernels' roofline, which are bound by FP32 issue rather than HBM. */
 int semb_probe_fp32(int32_t device, double* tflops);
 
+/* Diagnostic with no counterpart in the reference: runs the bounded barrier wait
+ * the search kernels use for their bulk copies on a barrier that nothing
+ * completes, with a limit of limit_us microseconds, and sets *timed_out to 1 when
+ * the wait gave up (as it must) -- the failure path that turns a lost copy into
+ * SEMB_E_TIMEOUT instead of a hung GPU, exercised without a fault. */
+int semb_selftest_wait(int32_t device, int64_t limit_us, int32_t* timed_out);
+
 /* Number of visible CUDA devices (0 when none); never fails. */
 int32_t semb_device_count(void);
 

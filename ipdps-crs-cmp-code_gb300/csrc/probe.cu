@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "common.h"
+#include "semb_kernels.cuh"
 
 namespace {
 
@@ -59,5 +60,39 @@ extern "C" int semb_probe_fp32(int32_t device, double* tflops) {
   SEMB_CUDA(e);
   const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
   *tflops = flops / (best * 1e-3) / 1e12;
+  return SEMB_OK;
+}
+
+namespace {
+
+// One CTA waits on a barrier phase that nothing completes, through the same
+// bounded wait the search kernels use for their bulk copies, and reports whether
+// the wait gave up (1) or completed (0).
+__global__ void k_wait_selftest(uint64_t limit_ns, int* timed_out) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    semb::mbar_init(&bar, 1);
+    semb::fence_mbar_init();
+  }
+  __syncthreads();
+  const bool ok = semb::wait_bar(&bar, 0, limit_ns);
+  if (threadIdx.x == 0) *timed_out = ok ? 0 : 1;
+}
+
+}  // namespace
+
+extern "C" int semb_selftest_wait(int32_t device, int64_t limit_us, int32_t* timed_out) {
+  if (!timed_out || limit_us <= 0 || limit_us > 10000000) return semb::fail(SEMB_E_ARG, "bad argument");
+  if (device < 0 || device >= semb_device_count()) return semb::fail(SEMB_E_NODEV, "device %d not available", device);
+  SEMB_CUDA(cudaSetDevice(device));
+  int* d = nullptr;
+  SEMB_CUDA(cudaMalloc(&d, sizeof(int)));
+  k_wait_selftest<<<1, 32>>>((uint64_t)limit_us * 1000ull, d);
+  cudaError_t e = cudaGetLastError();
+  int h = -1;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  SEMB_CUDA(e);
+  *timed_out = h;
   return SEMB_OK;
 }

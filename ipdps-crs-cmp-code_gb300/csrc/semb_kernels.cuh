@@ -395,12 +395,12 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
   }
 }
 
-// Bounded wait on a barrier phase; false when it did not complete within kWaitNs.
-__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity) {
+// Bounded wait on a barrier phase; false when it did not complete within limit_ns.
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, uint64_t limit_ns = kWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t_start = global_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t_start > kWaitNs) return false;
+    if (global_ns() - t_start > limit_ns) return false;
   }
   return true;
 }

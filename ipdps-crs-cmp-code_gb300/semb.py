@@ -35,7 +35,7 @@ EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
     "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
-    "semb_host_free", "semb_probe_fp32", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
+    "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
 
 
@@ -112,6 +112,7 @@ def lib():
         "semb_host_alloc": (C.c_int, [C.c_size_t, P]),
         "semb_host_free": (C.c_int, [P]),
         "semb_probe_fp32": (C.c_int, [i32, P]),
+        "semb_selftest_wait": (C.c_int, [i32, i64, P]),
         "semb_device_count": (i32, []),
         "semb_strerror": (C.c_char_p, [C.c_int]),
         "semb_last_error": (C.c_char_p, []),
@@ -347,6 +348,13 @@ def probe_fp32_tflops(device: int = 0) -> float:
     v = C.c_double()
     _check(lib().semb_probe_fp32(int(device), C.byref(v)), "semb_probe_fp32")
     return float(v.value)
+
+
+def selftest_wait(device: int = 0, limit_us: int = 20000) -> int:
+    """1 when the bounded device-side wait gave up on a barrier nothing completes."""
+    v = C.c_int32()
+    _check(lib().semb_selftest_wait(int(device), int(limit_us), C.byref(v)), "semb_selftest_wait")
+    return int(v.value)
 
 
 def device_count() -> int:

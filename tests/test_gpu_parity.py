@@ -73,3 +73,14 @@ def test_crs_neighbour_lists_match_reference_rule():
         off, lst = p.neighbours()
     assert np.array_equal(off, g["nbr_off"])
     assert np.array_equal(lst, g["nbr"])
+
+
+def test_bounded_wait_gives_up_and_device_stays_usable():
+    """A barrier nothing completes: the wait the search kernels use for their bulk
+    copies gives up after its limit, and the GPU keeps working afterwards."""
+    assert semb.selftest_wait(0, 20000) == 1
+    s = synth.cmp_survey(seed=26, ncmp=3, fold=6, ns=200, nc=8)
+    g = oracle.gather(s.headers, s.samples, "cmp", s.params["aph"])
+    (ctr, sem, stk), _ = _run(semb.CMP, g, s.params, mode=semb.PLAIN_F32)
+    ref = oracle.cmp(g, s.params, "f32")
+    assert np.array_equal(ctr, ref["ctr"])
