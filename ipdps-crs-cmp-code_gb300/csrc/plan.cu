@@ -258,6 +258,9 @@ int configure_variant(semb_plan* pl, int v) {
   std::vector<float> bounds((size_t)npass * 8, 0.f);
   const double s1 = pl->idt64, s2 = pl->idt64 * pl->idt64;
   for (int k = 0; k < npad; ++k) {
+    // padding slots repeat the last candidate's parameters (so the pass bounds are
+    // unchanged) with grid index -1: they are evaluated but never picked
+    const bool pad = k >= ncand;
     const int gi = pl->order[std::min(k, ncand - 1)];
     float4 c;
     if (form == FORM_PLAIN) {
@@ -266,7 +269,7 @@ int configure_variant(semb_plan* pl, int v) {
       c = make_float4((float)(pl->g64[3 * (size_t)gi] * s1), (float)(pl->g64[3 * (size_t)gi + 1] * s2),
                       (float)(pl->g64[3 * (size_t)gi + 2] * s2), 0.f);
     }
-    int32_t gbits = gi;
+    int32_t gbits = pad ? -1 : gi;
     std::memcpy(&c.w, &gbits, 4);
     cand[k] = c;
     float* bp = &bounds[(size_t)(k / cpp) * 8];

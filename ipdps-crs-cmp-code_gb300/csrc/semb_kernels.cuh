@@ -80,6 +80,7 @@ struct KParams {
   const int32_t* ap_tr;         // trace index of each entry
   const float4* ap_geo;         // (|dm|, dm^2, h, 0) per entry, FP32
   // candidates in search order, padded to npass*cpp; .w holds the grid index bits
+  // (-1 in padding slots)
   const float4* cand;
   const float* pass_bounds;     // [npass][8]: amin amax bmin bmax cmin cmax (raw units)
   int npass;
@@ -767,8 +768,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
           sem = ok ? __fdividef(acsq, den * mf) : kSent;
           stk = ok ? __fdividef(lin, (float)W * mf) : kSent;
         }
-        const int idx = __float_as_int(cand[r].w);
-        if (sem > 0.f && better(sem, idx, last_s, last_i)) {
+        const int idx = __float_as_int(cand[r].w);   // -1: padding slot
+        if (idx >= 0 && sem > 0.f && better(sem, idx, last_s, last_i)) {
           // sorted insert (descending semblance, ascending index)
           float cs = sem, ck = stk;
           int cidx = idx;
