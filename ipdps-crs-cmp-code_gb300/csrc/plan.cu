@@ -823,7 +823,7 @@ int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
   SEMB_CUDA(cudaMemcpy(d_sample, sample.data(), S * sizeof(int2), cudaMemcpyHostToDevice));
   int best = -1;
   double best_ms = 1e300;
-  for (int v = 0; v < 3; ++v) {
+  for (int v = 0; v < 4; ++v) {
     int rc = 0, minb = 0;
     if (ms_of_variant) ms_of_variant[v] = -1.0;
     if (!search_variant(p.method, form, pl->w, v, &rc, &minb)) continue;

@@ -1,10 +1,12 @@
 // Instantiation table of the search kernel for one (method, form).  For each
 // window width w = 2*tau+1 there are one or more variants (RC candidates per
-// thread, MINB resident CTAs per SM): more items per thread give more
+// thread, MINB resident CTAs per SM, staging layout): more items per thread give more
 // instruction-level parallelism and amortize per-trace work, more CTAs per SM
 // give the scheduler more warps to hide barrier and load latency.  The plan's
 // autotuner times the variants of its window on a sample of its own tasks and
-// keeps the fastest; variant 0 is the default.  RC values keep the per-item
+// keeps the fastest; variant 0 is the default.  The value/difference staging
+// layout (SD) saves one FP32 op per window sample for 50% more shared-memory
+// bytes per evaluation.  RC values keep the per-item
 // register state within 65536 / (256 * MINB) registers without spilling
 // (checked with -Xptxas -v).
 #pragma once
@@ -20,11 +22,11 @@ struct SearchEntry {
   int minb;
 };
 
-constexpr int kMaxVariants = 3;
+constexpr int kMaxVariants = 4;
 
-template <int METHOD, int FORM, int W, int RC, int MINB>
+template <int METHOD, int FORM, int W, int RC, int MINB, bool SD = false>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB>, RC, MINB};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, SD>, RC, MINB};
 }
 
 // Plain form: one variant per window.
@@ -62,11 +64,13 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 0) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 1) return entry<METHOD, FORM, 3, 4, 3>();
       if (variant == 2) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 6 : 8), 2>();
+      if (variant == 3) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, true>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 1) return entry<METHOD, FORM, 5, 4, 3>();
       if (variant == 2) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 6 : 4), 2>();
+      if (variant == 3) return entry<METHOD, FORM, 5, 6, 2, true>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;

@@ -364,9 +364,11 @@ __device__ __forceinline__ void issue_raw(const KParams& P, const ChunkMeta* met
   }
 }
 
-// Fast form, all warps: turn the landed raw windows into quad entries.  Lane l
-// builds entry k = k0 + l from raw samples k..k+3, so the warp's 16-byte stores
-// cover consecutive addresses (no bank conflicts).
+// Fast form, all warps: turn the landed raw windows into 16-byte entries, one per
+// sample k: (s_k, s_k+1, s_k+2, s_k+3) ("quads"), or with SD (s_k, s_k+1 - s_k,
+// s_k+1, s_k+2 - s_k+1) ("value/difference pairs").  Lane l builds entry k0 + l, so
+// the warp's 16-byte stores cover consecutive addresses (no bank conflicts).
+template <bool SD>
 __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta* meta, const int4* src,
                                               const unsigned char* raw, float4* bufq) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -376,22 +378,22 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
     if (si.z <= 0) continue;
     float4* dst = bufq + si.w;
     const int roff = si.w + 8 * e;
-    if (P.storage == STORE_F32) {
-      const float* r = reinterpret_cast<const float*>(raw) + roff;
-      for (int k = lane; k < si.z; k += 32) dst[k] = make_float4(r[k], r[k + 1], r[k + 2], r[k + 3]);
-    } else {
-      const float sc = meta->scale[e];
-      const uint16_t* r = reinterpret_cast<const uint16_t*>(raw) + roff;
-      const bool f16 = P.storage == STORE_F16;
-      for (int k = lane; k < si.z; k += 32) {
-        float v[4];
+    const float sc = P.storage == STORE_F32 ? 1.0f : meta->scale[e];
+    const float* r32 = reinterpret_cast<const float*>(raw) + roff;
+    const uint16_t* r16 = reinterpret_cast<const uint16_t*>(raw) + roff;
+    const bool f16 = P.storage == STORE_F16;
+    for (int k = lane; k < si.z; k += 32) {
+      float v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const uint32_t b = r[k + u];
+      for (int u = 0; u < (SD ? 3 : 4); ++u) {
+        if (P.storage == STORE_F32) {
+          v[u] = r32[k + u];
+        } else {
+          const uint32_t b = r16[k + u];
           v[u] = (f16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
         }
-        dst[k] = make_float4(v[0], v[1], v[2], v[3]);
       }
+      dst[k] = SD ? make_float4(v[0], v[1] - v[0], v[1], v[2] - v[1]) : make_float4(v[0], v[1], v[2], v[3]);
     }
   }
 }
@@ -462,7 +464,7 @@ __host__ __device__ constexpr size_t kahan_bytes(int form, int rc) {
 // ---------------------------------------------------------------------------
 // The search kernel.
 
-template <int METHOD, int FORM, int W, int RC, int MINB>
+template <int METHOD, int FORM, int W, int RC, int MINB, bool SD>
 __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage);
@@ -628,13 +630,33 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
                 return fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
               };
               auto accumulate = [&](int r, uint32_t a, float x) {
-                float sv[W + 1];
-                load_window<W>(a, sv);
+                if (SD) {
+                  // entries (s_k, d_k, s_k+1, d_k+1): v_j = s_j + x * d_j
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                  const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
-                  fa[r].num[j] += v;
-                  fa[r].den_c = fmaf(v, v, fa[r].den_c);
+                  for (int p = 0; p < W / 2; ++p) {
+                    const float4 ev = lds128(a + 32u * p);
+                    const float v0 = fmaf(ev.y, x, ev.x);
+                    const float v1 = fmaf(ev.w, x, ev.z);
+                    fa[r].num[2 * p] += v0;
+                    fa[r].num[2 * p + 1] += v1;
+                    fa[r].den_c = fmaf(v0, v0, fa[r].den_c);
+                    fa[r].den_c = fmaf(v1, v1, fa[r].den_c);
+                  }
+                  if (W & 1) {
+                    const float2 ev = lds64(a + 16u * (W - 1));
+                    const float v = fmaf(ev.y, x, ev.x);
+                    fa[r].num[W - 1] += v;
+                    fa[r].den_c = fmaf(v, v, fa[r].den_c);
+                  }
+                } else {
+                  float sv[W + 1];
+                  load_window<W>(a, sv);
+#pragma unroll
+                  for (int j = 0; j < W; ++j) {
+                    const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
+                    fa[r].num[j] += v;
+                    fa[r].den_c = fmaf(v, v, fa[r].den_c);
+                  }
                 }
               };
               if (meta->inrange[e]) {
@@ -718,14 +740,15 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
         while (ap_pos < ap_end) {
           ChunkMeta* mc = meta_at(cur);
           const int n = mc->n;
+          // every thread observes the copies' completion itself; the timeout vote
+          // rides on the barrier after the conversion
           const bool ok = wait_bar(bars + cur, (phases >> cur) & 1u);
           phases ^= 1u << cur;
-          if (__syncthreads_or(!ok)) {
+          if (ok) convert_chunk<SD>(P, mc, srcs + cur * kMaxChunk, raw_at(cur), bufq);
+          if (__syncthreads_or(!ok)) {   // entries ready; raw buffer cur free
             if (threadIdx.x == 0) atomicOr(P.status, ST_TIMEOUT);
             return;
           }
-          convert_chunk(P, mc, srcs + cur * kMaxChunk, raw_at(cur), bufq);
-          __syncthreads();   // quads ready; raws[cur] free
           const int64_t next = ap_pos + n;
           if (warp == 0) {
             ChunkMeta* mn = meta_at(cur ^ 1);
