@@ -26,7 +26,8 @@ namespace semb {
 // Launchers of the search kernel instantiations (kernels_*.cu).
 int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
-int search_variant(int method, int form, int w, int variant, int* rc, int* minb);
+int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun);
+constexpr int kVariantSlots = 6;
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);
@@ -238,30 +239,44 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
 int configure_variant(semb_plan* pl, int v) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  int rc = 0, minb = 0;
-  if (!search_variant(p.method, form, pl->w, v, &rc, &minb))
+  int rc = 0, minb = 0, brun = 0;
+  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun))
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
   const int ncand = pl->ncand;
+  // search order; a negative slot -1-g marks padding that repeats candidate g.
+  // B-run variants pad each (A, C) group's run of nb B values to a multiple of RC
+  // so that every thread's RC candidates share A and C.
+  std::vector<int> slots;
+  if (brun && p.method == SEMB_CRS) {
+    const int nbp = (p.nb + rc - 1) / rc * rc;
+    slots.reserve((size_t)p.na * p.nc * nbp);
+    for (int g0 = 0; g0 < ncand; g0 += p.nb)
+      for (int k = 0; k < nbp; ++k) slots.push_back(k < p.nb ? pl->order[g0 + k] : -1 - pl->order[g0 + p.nb - 1]);
+  } else {
+    slots = pl->order;
+  }
+  const int nslots = (int)slots.size();
   int best_nw = 8, best_tot = INT32_MAX;
   for (int nw = 8; nw >= 4; --nw) {
     const int per = nw * rc;
-    const int tot = ((ncand + per - 1) / per) * per;
+    const int tot = ((nslots + per - 1) / per) * per;
     if (tot < best_tot) {
       best_tot = tot;
       best_nw = nw;
     }
   }
   const int cpp = best_nw * rc;
-  const int npass = (ncand + cpp - 1) / cpp;
+  const int npass = (nslots + cpp - 1) / cpp;
   const int npad = npass * cpp;
   std::vector<float4> cand(npad);
   std::vector<float> bounds((size_t)npass * 8, 0.f);
   const double s1 = pl->idt64, s2 = pl->idt64 * pl->idt64;
   for (int k = 0; k < npad; ++k) {
-    // padding slots repeat the last candidate's parameters (so the pass bounds are
+    // padding slots repeat a real candidate's parameters (so the pass bounds are
     // unchanged) with grid index -1: they are evaluated but never picked
-    const bool pad = k >= ncand;
-    const int gi = pl->order[std::min(k, ncand - 1)];
+    const int sv = slots[std::min(k, nslots - 1)];
+    const bool pad = k >= nslots || sv < 0;
+    const int gi = sv >= 0 ? sv : -1 - sv;
     float4 c;
     if (form == FORM_PLAIN) {
       c = make_float4(pl->ga[gi], pl->gb[gi], pl->gc[gi], 0.f);
@@ -802,6 +817,17 @@ int semb_plan_neighbours(semb_plan* pl, int32_t* off, int32_t* list, int64_t* n_
   return SEMB_OK;
 }
 
+int semb_plan_set_variant(semb_plan* pl, int32_t variant) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_set_variant before semb_plan_upload");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  const int form = pl->p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
+  int rc = 0, minb = 0, brun = 0;
+  if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun))
+    return fail(SEMB_E_ARG, "no search kernel variant %d for this plan", variant);
+  return configure_variant(pl, variant);
+}
+
 int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
   if (!pl) return fail(SEMB_E_ARG, "null argument");
   if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_autotune before semb_plan_upload");
@@ -823,10 +849,10 @@ int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
   SEMB_CUDA(cudaMemcpy(d_sample, sample.data(), S * sizeof(int2), cudaMemcpyHostToDevice));
   int best = -1;
   double best_ms = 1e300;
-  for (int v = 0; v < 4; ++v) {
-    int rc = 0, minb = 0;
+  for (int v = 0; v < kVariantSlots; ++v) {
+    int rc = 0, minb = 0, brun = 0;
     if (ms_of_variant) ms_of_variant[v] = -1.0;
-    if (!search_variant(p.method, form, pl->w, v, &rc, &minb)) continue;
+    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun)) continue;
     SEMB_TRY(configure_variant(pl, v));
     KParams P = make_kparams(pl);
     P.tasks = d_sample;

@@ -20,13 +20,14 @@ struct SearchEntry {
   const void* fn;
   int rc;
   int minb;
+  int brun;   // candidates laid out as B runs of RC (CRS)
 };
 
-constexpr int kMaxVariants = 4;
+constexpr int kMaxVariants = 6;
 
-template <int METHOD, int FORM, int W, int RC, int MINB, bool SD = false>
+template <int METHOD, int FORM, int W, int RC, int MINB, bool SD = false, bool BRUN = false>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, SD>, RC, MINB};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, SD, BRUN>, RC, MINB, BRUN ? 1 : 0};
 }
 
 // Plain form: one variant per window.
@@ -39,7 +40,7 @@ SearchEntry plain_entry() {
 template <int METHOD, int FORM>
 SearchEntry search_entry(int w, int variant) {
   if (FORM == FORM_PLAIN) {
-    if (variant != 0) return {nullptr, 0, 0};
+    if (variant != 0) return {nullptr, 0, 0, 0};
     switch (w) {
       case 1: return plain_entry<METHOD, 1>();
       case 3: return plain_entry<METHOD, 3>();
@@ -51,7 +52,7 @@ SearchEntry search_entry(int w, int variant) {
       case 13: return plain_entry<METHOD, 13>();
       case 15: return plain_entry<METHOD, 15>();
 #endif
-      default: return {nullptr, 0, 0};
+      default: return {nullptr, 0, 0, 0};
     }
   }
   // fast form
@@ -59,18 +60,24 @@ SearchEntry search_entry(int w, int variant) {
     case 1:
       if (variant == 0) return entry<METHOD, FORM, 1, 8, 2>();
       if (variant == 1) return entry<METHOD, FORM, 1, 4, 3>();
+      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 1, 7, 2, false, true>();
+      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 1, 8, 2, false, true>();
       break;
     case 3:
       if (variant == 0) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 1) return entry<METHOD, FORM, 3, 4, 3>();
       if (variant == 2) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 6 : 8), 2>();
       if (variant == 3) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, true>();
+      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 3, 7, 2, true, true>();
+      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 3, 8, 2, false, true>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 1) return entry<METHOD, FORM, 5, 4, 3>();
       if (variant == 2) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 6 : 4), 2>();
       if (variant == 3) return entry<METHOD, FORM, 5, 6, 2, true>();
+      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 5, 7, 2, false, true>();
+      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 5, 8, 2, false, true>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;
@@ -81,7 +88,7 @@ SearchEntry search_entry(int w, int variant) {
 #endif
     default: break;
   }
-  return {nullptr, 0, 0};
+  return {nullptr, 0, 0, 0};
 }
 
 }  // namespace semb

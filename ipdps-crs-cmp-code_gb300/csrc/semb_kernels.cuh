@@ -43,7 +43,9 @@
 //          in sample units (candidates pre-scaled by idt), the stack taken from
 //          sum_j num_j, and the energy accumulated per chunk and folded into a
 //          Kahan-compensated total; keeps the top-4 candidates per t0 for the
-//          FP64 re-pick.
+//          FP64 re-pick.  With BRUN (CRS), the plan lays the candidates out so that
+//          each thread's RC candidates are consecutive B values of one (A, C) pair,
+//          and the A and C terms of the traveltime are computed once per trace.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -464,7 +466,7 @@ __host__ __device__ constexpr size_t kahan_bytes(int form, int rc) {
 // ---------------------------------------------------------------------------
 // The search kernel.
 
-template <int METHOD, int FORM, int W, int RC, int MINB, bool SD>
+template <int METHOD, int FORM, int W, int RC, int MINB, bool SD, bool BRUN>
 __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage);
@@ -624,8 +626,15 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
               }
             } else {
               // t2 in samples^2 for item r on this trace
+              // B-run candidates share A and C: (t0 + A|dm|)^2 + C h once per trace
+              float q0 = 0.f;
+              if (BRUN && METHOD == METHOD_CRS) {
+                const float u0 = fmaf(ca[0], g.x, Tsmp);
+                q0 = fmaf(u0, u0, cc[0] * g.z);
+              }
               auto t2_of = [&](int r) {
                 if (METHOD == METHOD_CMP) return fmaf(cc[r], g.z, T2smp);
+                if (BRUN) return fmaf(cb[r], g.y, q0);
                 const float u = fmaf(ca[r], g.x, Tsmp);
                 return fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
               };

@@ -34,7 +34,7 @@ OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODE
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
-    "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
+    "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
     "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
 
@@ -107,6 +107,7 @@ def lib():
         "semb_plan_stats": (C.c_int, [P, P]),
         "semb_neighbours_noalloc": (C.c_int, [P, P, P, P, P, i32, i32, P, P, i64, P, P]),
         "semb_plan_autotune": (C.c_int, [P, P, P]),
+        "semb_plan_set_variant": (C.c_int, [P, i32]),
         "semb_plan_use_graph": (C.c_int, [P, i32]),
         "semb_plan_destroy": (C.c_int, [P]),
         "semb_host_alloc": (C.c_int, [C.c_size_t, P]),
@@ -285,9 +286,12 @@ class Plan:
         """Pick the fastest search-kernel variant on a sample of this plan's tasks.
         Returns (chosen variant, [sample ms per variant, -1 when absent])."""
         v = C.c_int32()
-        ms = (C.c_double * 4)()
+        ms = (C.c_double * 6)()
         _check(lib().semb_plan_autotune(self._h, C.byref(v), ms), "semb_plan_autotune")
         return int(v.value), [float(x) for x in ms]
+
+    def set_variant(self, v: int) -> None:
+        _check(lib().semb_plan_set_variant(self._h, int(v)), "semb_plan_set_variant")
 
     def stats(self) -> dict:
         s = SembStats()

@@ -147,3 +147,28 @@ def test_reupload_and_rerun_are_stable():
             outs.append(plan.download())
     for x, y in zip(*outs):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("case", ["cmp_line", "crs_line", "crs_uneven_w5"])
+def test_every_variant_agrees_with_the_default(case):
+    """Each search-kernel variant (items per thread, CTAs per SM, staging and
+    candidate layouts) gives the default variant's picks and semblances."""
+    meta, h, s, path = G.load(case)
+    method, p = meta["method"], meta["params"]
+    sv = semb.Survey.load(path, METHOD[method], p["aph"])
+    with semb.Plan(semb.params(METHOD[method], mode=semb.BATCHED, repick=semb.REPICK_OFF, **p)) as plan:
+        plan.upload(sv.view())
+        plan.run()
+        base = plan.download()
+        tried = 0
+        for v in range(1, 6):
+            try:
+                plan.set_variant(v)
+            except semb.SembError:
+                continue
+            tried += 1
+            plan.run()
+            out = plan.download()
+            assert np.mean(out[0] == base[0]) >= 0.995, v
+            np.testing.assert_allclose(out[1], base[1], atol=2e-6, rtol=1e-5)
+        assert tried >= 1
