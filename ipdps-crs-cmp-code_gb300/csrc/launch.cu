@@ -17,12 +17,13 @@ static SearchEntry lookup(int method, int form, int w, int v) {
   return form == FORM_PLAIN ? search_entry_crs_plain(w, v) : search_entry_crs_fast(w, v);
 }
 
-int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun) {
+int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt) {
   if (v < 0 || v >= kMaxVariants) return 0;
   SearchEntry e = lookup(method, form, w, v);
   *rc = e.rc;
   *minb = e.minb;
   *brun = e.brun;
+  *nt = e.nt;
   return e.fn != nullptr;
 }
 

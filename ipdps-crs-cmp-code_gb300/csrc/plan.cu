@@ -26,8 +26,8 @@ namespace semb {
 // Launchers of the search kernel instantiations (kernels_*.cu).
 int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
-int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun);
-constexpr int kVariantSlots = 6;
+int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt);
+constexpr int kVariantSlots = 8;
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);
@@ -239,8 +239,8 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
 int configure_variant(semb_plan* pl, int v) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  int rc = 0, minb = 0, brun = 0;
-  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun))
+  int rc = 0, minb = 0, brun = 0, nt = 0;
+  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt))
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
   const int ncand = pl->ncand;
   // search order; a negative slot -1-g marks padding that repeats candidate g.
@@ -256,8 +256,8 @@ int configure_variant(semb_plan* pl, int v) {
     slots = pl->order;
   }
   const int nslots = (int)slots.size();
-  int best_nw = 8, best_tot = INT32_MAX;
-  for (int nw = 8; nw >= 4; --nw) {
+  int best_nw = nt / 32, best_tot = INT32_MAX;
+  for (int nw = nt / 32; nw >= 4; --nw) {
     const int per = nw * rc;
     const int tot = ((nslots + per - 1) / per) * per;
     if (tot < best_tot) {
@@ -312,9 +312,9 @@ int configure_variant(semb_plan* pl, int v) {
   const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
   const size_t budget = (227 * 1024) / minb - 1024;
   int cap = form == FORM_PLAIN ? 32768 : 8192;
-  while (cap > 64 && smem_layout(form, rc, cap, store).total > budget) cap -= 64;
+  while (cap > 64 && smem_layout(form, rc, cap, store, nt).total > budget) cap -= 64;
   if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
-  const size_t smem = smem_layout(form, rc, cap, store).total;
+  const size_t smem = smem_layout(form, rc, cap, store, nt).total;
   if (smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", pl->ns);
   int occ = 0;
   SEMB_TRY(search_occupancy(p.method, form, pl->w, v, best_nw, smem, &occ));
@@ -822,8 +822,8 @@ int semb_plan_set_variant(semb_plan* pl, int32_t variant) {
   if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_set_variant before semb_plan_upload");
   SEMB_CUDA(cudaSetDevice(pl->device));
   const int form = pl->p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  int rc = 0, minb = 0, brun = 0;
-  if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun))
+  int rc = 0, minb = 0, brun = 0, nt = 0;
+  if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun, &nt))
     return fail(SEMB_E_ARG, "no search kernel variant %d for this plan", variant);
   return configure_variant(pl, variant);
 }
@@ -850,9 +850,9 @@ int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
   int best = -1;
   double best_ms = 1e300;
   for (int v = 0; v < kVariantSlots; ++v) {
-    int rc = 0, minb = 0, brun = 0;
+    int rc = 0, minb = 0, brun = 0, nt = 0;
     if (ms_of_variant) ms_of_variant[v] = -1.0;
-    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun)) continue;
+    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt)) continue;
     SEMB_TRY(configure_variant(pl, v));
     KParams P = make_kparams(pl);
     P.tasks = d_sample;

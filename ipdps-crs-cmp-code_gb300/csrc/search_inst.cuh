@@ -1,8 +1,10 @@
 // Instantiation table of the search kernel for one (method, form).  For each
 // window width w = 2*tau+1 there are one or more variants (RC candidates per
-// thread, MINB resident CTAs per SM, staging layout): more items per thread give more
+// thread, MINB resident CTAs per SM of NT threads, staging layout, candidate
+// layout): more items per thread give more
 // instruction-level parallelism and amortize per-trace work, more CTAs per SM
-// give the scheduler more warps to hide barrier and load latency.  The plan's
+// give the scheduler more warps to hide barrier and load latency, and smaller
+// CTAs let the others fill the cycles one of them spends at a barrier.  The plan's
 // autotuner times the variants of its window on a sample of its own tasks and
 // keeps the fastest; variant 0 is the default.  The value/difference staging
 // layout (SD) saves one FP32 op per window sample for 50% more shared-memory
@@ -21,13 +23,14 @@ struct SearchEntry {
   int rc;
   int minb;
   int brun;   // candidates laid out as B runs of RC (CRS)
+  int nt;     // threads per CTA
 };
 
-constexpr int kMaxVariants = 6;
+constexpr int kMaxVariants = 8;
 
-template <int METHOD, int FORM, int W, int RC, int MINB, bool SD = false, bool BRUN = false>
+template <int METHOD, int FORM, int W, int RC, int MINB, bool SD = false, bool BRUN = false, int NT = 256>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, SD, BRUN>, RC, MINB, BRUN ? 1 : 0};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, SD, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT};
 }
 
 // Plain form: one variant per window.
@@ -40,7 +43,7 @@ SearchEntry plain_entry() {
 template <int METHOD, int FORM>
 SearchEntry search_entry(int w, int variant) {
   if (FORM == FORM_PLAIN) {
-    if (variant != 0) return {nullptr, 0, 0, 0};
+    if (variant != 0) return {nullptr, 0, 0, 0, 0};
     switch (w) {
       case 1: return plain_entry<METHOD, 1>();
       case 3: return plain_entry<METHOD, 3>();
@@ -52,7 +55,7 @@ SearchEntry search_entry(int w, int variant) {
       case 13: return plain_entry<METHOD, 13>();
       case 15: return plain_entry<METHOD, 15>();
 #endif
-      default: return {nullptr, 0, 0, 0};
+      default: return {nullptr, 0, 0, 0, 0};
     }
   }
   // fast form
@@ -62,6 +65,7 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 1) return entry<METHOD, FORM, 1, 4, 3>();
       if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 1, 7, 2, false, true>();
       if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 1, 8, 2, false, true>();
+      if (variant == 6) return entry<METHOD, FORM, 1, 8, 4, false, false, 128>();
       break;
     case 3:
       if (variant == 0) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -70,6 +74,8 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 3) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, true>();
       if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 3, 7, 2, true, true>();
       if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 3, 8, 2, false, true>();
+      if (variant == 6) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, false, METHOD == METHOD_CRS, 128>();
+      if (variant == 7) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, true, METHOD == METHOD_CRS, 128>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -78,6 +84,7 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 3) return entry<METHOD, FORM, 5, 6, 2, true>();
       if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 5, 7, 2, false, true>();
       if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 5, 8, 2, false, true>();
+      if (variant == 6) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 7), 4, false, METHOD == METHOD_CRS, 128>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;
@@ -88,7 +95,7 @@ SearchEntry search_entry(int w, int variant) {
 #endif
     default: break;
   }
-  return {nullptr, 0, 0, 0};
+  return {nullptr, 0, 0, 0, 0};
 }
 
 }  // namespace semb

@@ -63,7 +63,7 @@ constexpr int kMaxChunk = 128;   // aperture traces staged per chunk
 constexpr int kMargin = 2;       // extra samples on each side of a staged window
 constexpr int kTopK = 4;
 constexpr int kZeroSlots = 16;   // zero block after the staging buffer (floats or entries)
-constexpr int kMaxThreads = 256; // CTA size limit of the search kernel
+constexpr int kMaxThreads = 256; // CTA size limit of the search kernel (variants use 128 or 256)
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier wait (2 s), then error
 
 // Device status word bits.
@@ -187,8 +187,8 @@ constexpr size_t kMetaBytes = ((sizeof(ChunkMeta) + 127) / 128) * 128;
 //   [0, 64)   two mbarriers and control words
 //   meta[2]   chunk metadata (the fast form alternates two chunks)
 //   src[2]    per-entry copy descriptors (trace, first sample, length, offset)
-//   top-K     per-thread running picks [3][K][kMaxThreads]
-//   kahan     fast form: per-item compensated energy totals [2][RC][kMaxThreads]
+//   top-K     per-thread running picks [3][K][nt]
+//   kahan     fast form: per-item compensated energy totals [2][RC][nt]
 //   buf       staging buffer: cap floats (plain) or cap 16-byte quads (fast),
 //             followed by kZeroSlots zeroed slots read by out-of-range items
 //   raw[2]    fast form: the raw windows of two chunks as stored in HBM
@@ -199,14 +199,14 @@ struct SmemLayout {
 
 __host__ __device__ inline size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
 
-__host__ __device__ inline SmemLayout smem_layout(int form, int rc, int cap, int storage) {
+__host__ __device__ inline SmemLayout smem_layout(int form, int rc, int cap, int storage, int nt) {
   const int K = form == 1 ? 4 : 1;
   SmemLayout L;
   L.meta = 64;
   L.src = L.meta + 2 * kMetaBytes;
   L.tops = L.src + 2 * kMaxChunk * sizeof(int4);
-  L.kahan = L.tops + align128(3 * (size_t)K * kMaxThreads * 4);
-  L.buf = L.kahan + (form == 1 ? 2 * (size_t)rc * kMaxThreads * 4 : 0);
+  L.kahan = L.tops + align128(3 * (size_t)K * nt * 4);
+  L.buf = L.kahan + (form == 1 ? 2 * (size_t)rc * nt * 4 : 0);
   const size_t unit = form == 1 ? 16 : 4;
   const size_t raw_end = L.buf + align128(((size_t)cap + kZeroSlots) * unit);
   if (form == 1) {
@@ -458,29 +458,26 @@ struct FastAcc {
   int M;            // and its compensation live in shared memory (kahan_hi/lo)
 };
 
-// Shared memory of the fast form's Kahan totals: [2][RC][kMaxThreads] floats.
-__host__ __device__ constexpr size_t kahan_bytes(int form, int rc) {
-  return form == FORM_FAST ? 2 * (size_t)rc * kMaxThreads * 4 : 0;
-}
+
 
 // ---------------------------------------------------------------------------
 // The search kernel.
 
-template <int METHOD, int FORM, int W, int RC, int MINB, bool SD, bool BRUN>
-__global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams P) {
+template <int METHOD, int FORM, int W, int RC, int MINB, bool SD, bool BRUN, int NT>
+__global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage);
+  const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage, NT);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);   // [2]
   int* ctl = reinterpret_cast<int*>(smem_raw + 16);
   ChunkMeta* metas = reinterpret_cast<ChunkMeta*>(smem_raw + L.meta);   // [2], stride kMetaBytes
   int4* srcs = reinterpret_cast<int4*>(smem_raw + L.src);               // [2][kMaxChunk]
-  // running top-K per thread, [K][kMaxThreads] (semblance, grid index, stack)
+  // running top-K per thread, [K][NT] (semblance, grid index, stack)
   constexpr int K = (FORM == FORM_FAST) ? kTopK : 1;
   float* top_s = reinterpret_cast<float*>(smem_raw + L.tops);
-  int* top_i = reinterpret_cast<int*>(top_s + K * kMaxThreads);
-  float* top_k = top_s + 2 * K * kMaxThreads;
-  float* kahan_hi = reinterpret_cast<float*>(smem_raw + L.kahan);   // fast form: [RC][kMaxThreads]
-  float* kahan_lo = kahan_hi + RC * kMaxThreads;
+  int* top_i = reinterpret_cast<int*>(top_s + K * NT);
+  float* top_k = top_s + 2 * K * NT;
+  float* kahan_hi = reinterpret_cast<float*>(smem_raw + L.kahan);   // fast form: [RC][NT]
+  float* kahan_lo = kahan_hi + RC * NT;
   float* buf = reinterpret_cast<float*>(smem_raw + L.buf);
   float4* bufq = reinterpret_cast<float4*>(buf);
   auto raw_at = [&](int i) { return smem_raw + L.raw0 + (size_t)i * (L.raw1 - L.raw0); };
@@ -540,9 +537,9 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
     // admission threshold (the K-th entry) in registers
 #pragma unroll
     for (int q = 0; q < K; ++q) {
-      top_s[q * kMaxThreads + threadIdx.x] = 0.f;
-      top_i[q * kMaxThreads + threadIdx.x] = 0x7fffffff;
-      top_k[q * kMaxThreads + threadIdx.x] = 0.f;
+      top_s[q * NT + threadIdx.x] = 0.f;
+      top_i[q * NT + threadIdx.x] = 0x7fffffff;
+      top_k[q * NT + threadIdx.x] = 0.f;
     }
     float last_s = 0.f;
     int last_i = 0x7fffffff;
@@ -583,8 +580,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
         } else {
           fa[r].den_c = 0.f;
           fa[r].M = 0;
-          kahan_hi[r * kMaxThreads + threadIdx.x] = 0.f;
-          kahan_lo[r * kMaxThreads + threadIdx.x] = 0.f;
+          kahan_hi[r * NT + threadIdx.x] = 0.f;
+          kahan_lo[r * NT + threadIdx.x] = 0.f;
         }
       }
 
@@ -705,7 +702,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
 #pragma unroll
             for (int r = 0; r < RC; ++r) {
               // Kahan: fold this chunk's energy into the compensated total
-              const int o = r * kMaxThreads + threadIdx.x;
+              const int o = r * NT + threadIdx.x;
               const float hi = kahan_hi[o], lo = kahan_lo[o];
               const float yv = fa[r].den_c - lo;
               const float tv = hi + yv;
@@ -793,7 +790,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
             acsq = fmaf(fa[r].num[j], fa[r].num[j], acsq);
             lin += fa[r].num[j];
           }
-          const float den = kahan_hi[r * kMaxThreads + threadIdx.x] - kahan_lo[r * kMaxThreads + threadIdx.x];
+          const float den = kahan_hi[r * NT + threadIdx.x] - kahan_lo[r * NT + threadIdx.x];
           const float mf = (float)fa[r].M;
           const int err = napert - fa[r].M;
           const bool ok = ((double)den > 1e-13) && (fa[r].M > 0) && (err < 2);
@@ -807,7 +804,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
           int cidx = idx;
 #pragma unroll
           for (int q = 0; q < K; ++q) {
-            const int o = q * kMaxThreads + threadIdx.x;
+            const int o = q * NT + threadIdx.x;
             const float bs = top_s[o];
             const int bi = top_i[o];
             if (better(cs, cidx, bs, bi)) {
@@ -820,8 +817,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
               ck = bk;
             }
           }
-          last_s = top_s[(K - 1) * kMaxThreads + threadIdx.x];
-          last_i = top_i[(K - 1) * kMaxThreads + threadIdx.x];
+          last_s = top_s[(K - 1) * NT + threadIdx.x];
+          last_i = top_i[(K - 1) * NT + threadIdx.x];
         }
       }
     }
@@ -840,9 +837,9 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) semb_search_kernel(KParams 
       }
       for (int w2 = 0; w2 < nwarps; ++w2) {
         for (int q2 = 0; q2 < K; ++q2) {
-          float cs = top_s[q2 * kMaxThreads + w2 * 32 + lane];
-          int cidx = top_i[q2 * kMaxThreads + w2 * 32 + lane];
-          float ck = top_k[q2 * kMaxThreads + w2 * 32 + lane];
+          float cs = top_s[q2 * NT + w2 * 32 + lane];
+          int cidx = top_i[q2 * NT + w2 * 32 + lane];
+          float ck = top_k[q2 * NT + w2 * 32 + lane];
           if (!(cs > 0.f)) continue;
 #pragma unroll
           for (int q = 0; q < K; ++q) {

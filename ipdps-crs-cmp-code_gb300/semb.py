@@ -286,7 +286,7 @@ class Plan:
         """Pick the fastest search-kernel variant on a sample of this plan's tasks.
         Returns (chosen variant, [sample ms per variant, -1 when absent])."""
         v = C.c_int32()
-        ms = (C.c_double * 6)()
+        ms = (C.c_double * 8)()
         _check(lib().semb_plan_autotune(self._h, C.byref(v), ms), "semb_plan_autotune")
         return int(v.value), [float(x) for x in ms]
 
