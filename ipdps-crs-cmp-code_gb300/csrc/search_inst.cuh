@@ -42,7 +42,7 @@ SearchEntry plain_entry() {
 
 template <int METHOD, int FORM>
 SearchEntry search_entry(int w, int variant) {
-  if (FORM == FORM_PLAIN) {
+  if constexpr (FORM == FORM_PLAIN) {
     if (variant != 0) return {nullptr, 0, 0, 0, 0};
     switch (w) {
       case 1: return plain_entry<METHOD, 1>();
@@ -57,7 +57,7 @@ SearchEntry search_entry(int w, int variant) {
 #endif
       default: return {nullptr, 0, 0, 0, 0};
     }
-  }
+  } else {
   // fast form
   switch (w) {
     case 1:
@@ -96,6 +96,7 @@ SearchEntry search_entry(int w, int variant) {
     default: break;
   }
   return {nullptr, 0, 0, 0, 0};
+  }
 }
 
 }  // namespace semb
