@@ -29,7 +29,10 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 1
+#define SEMB_ABI_VERSION 2
+
+/* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
+#define SEMB_MAX_VARIANTS 12
 
 /* Methods. */
 enum { SEMB_CMP = 0, SEMB_CRS = 1 };
@@ -222,13 +225,14 @@ int semb_plan_stats(const semb_plan* plan, semb_stats* out);
 /* Time each variant of the search kernel available for this plan's window
  * (candidates per thread x CTA size x resident CTAs per SM x staging layout x
  * candidate layout) on a strided sample of the plan's own work queue and keep the fastest
- * for later runs.  *chosen gets the variant, ms_of_variant[0..7] (optional) the
+ * for later runs.  *chosen gets the variant, ms_of_variant[0..SEMB_MAX_VARIANTS-1]
+ * (optional) the
  * sample times (-1: no such variant).
  * No counterpart in the reference, which has one fixed launch shape
  * (CRS/CUDA/src/main.cu:45-51, 439). */
 int semb_plan_autotune(semb_plan* plan, int32_t* chosen, double* ms_of_variant);
 
-/* Use search-kernel variant `variant` (0..7) for later runs; SEMB_E_ARG when this
+/* Use search-kernel variant `variant` (0..SEMB_MAX_VARIANTS-1) for later runs; SEMB_E_ARG when this
  * plan's window and form have no such variant.  No counterpart in the reference. */
 int semb_plan_set_variant(semb_plan* plan, int32_t variant);
 

@@ -27,7 +27,7 @@ namespace semb {
 int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
 int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt);
-constexpr int kVariantSlots = 8;
+constexpr int kVariantSlots = SEMB_MAX_VARIANTS;
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);

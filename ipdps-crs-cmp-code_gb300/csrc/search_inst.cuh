@@ -7,8 +7,9 @@
 // CTAs let the others fill the cycles one of them spends at a barrier.  The plan's
 // autotuner times the variants of its window on a sample of its own tasks and
 // keeps the fastest; variant 0 is the default.  The value/difference staging
-// layout (SD) saves one FP32 op per window sample for 50% more shared-memory
-// bytes per evaluation.  RC values keep the per-item
+// layout (LAY_SD) saves one FP32 op per window sample for 50% more shared-memory
+// bytes per evaluation; the packed layout (LAY_P2) does two window samples per
+// FP32x2 instruction.  RC values keep the per-item
 // register state within 65536 / (256 * MINB) registers without spilling
 // (checked with -Xptxas -v).
 #pragma once
@@ -26,11 +27,11 @@ struct SearchEntry {
   int nt;     // threads per CTA
 };
 
-constexpr int kMaxVariants = 8;
+constexpr int kMaxVariants = SEMB_MAX_VARIANTS;
 
-template <int METHOD, int FORM, int W, int RC, int MINB, bool SD = false, bool BRUN = false, int NT = 256>
+template <int METHOD, int FORM, int W, int RC, int MINB, int LAY = LAY_QUAD, bool BRUN = false, int NT = 256>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, SD, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT};
 }
 
 // Plain form: one variant per window.
@@ -63,28 +64,34 @@ SearchEntry search_entry(int w, int variant) {
     case 1:
       if (variant == 0) return entry<METHOD, FORM, 1, 8, 2>();
       if (variant == 1) return entry<METHOD, FORM, 1, 4, 3>();
-      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 1, 7, 2, false, true>();
-      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 1, 8, 2, false, true>();
-      if (variant == 6) return entry<METHOD, FORM, 1, 8, 4, false, false, 128>();
+      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 1, 7, 2, LAY_QUAD, true>();
+      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 1, 8, 2, LAY_QUAD, true>();
+      if (variant == 6) return entry<METHOD, FORM, 1, 8, 4, LAY_QUAD, false, 128>();
       break;
     case 3:
       if (variant == 0) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 1) return entry<METHOD, FORM, 3, 4, 3>();
       if (variant == 2) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 6 : 8), 2>();
-      if (variant == 3) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, true>();
-      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 3, 7, 2, true, true>();
-      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 3, 8, 2, false, true>();
-      if (variant == 6) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, false, METHOD == METHOD_CRS, 128>();
-      if (variant == 7) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, true, METHOD == METHOD_CRS, 128>();
+      if (variant == 3) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_SD>();
+      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 3, 7, 2, LAY_SD, true>();
+      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 3, 8, 2, LAY_QUAD, true>();
+      if (variant == 6) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_QUAD, METHOD == METHOD_CRS, 128>();
+      if (variant == 7) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_SD, METHOD == METHOD_CRS, 128>();
+      if (variant == 8) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2>();
+      if (variant == 9) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_P2, METHOD == METHOD_CRS, 128>();
+      if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 3, 8, 2, LAY_P2, true>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 1) return entry<METHOD, FORM, 5, 4, 3>();
       if (variant == 2) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 6 : 4), 2>();
-      if (variant == 3) return entry<METHOD, FORM, 5, 6, 2, true>();
-      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 5, 7, 2, false, true>();
-      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 5, 8, 2, false, true>();
-      if (variant == 6) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 7), 4, false, METHOD == METHOD_CRS, 128>();
+      if (variant == 3) return entry<METHOD, FORM, 5, 6, 2, LAY_SD>();
+      if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 5, 7, 2, LAY_QUAD, true>();
+      if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 5, 8, 2, LAY_QUAD, true>();
+      if (variant == 6) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_QUAD, METHOD == METHOD_CRS, 128>();
+      if (variant == 8) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2>();
+      if (variant == 9) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_P2, METHOD == METHOD_CRS, 128>();
+      if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 5, 8, 2, LAY_P2, true>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;

@@ -173,15 +173,31 @@ __device__ __forceinline__ bool better(float s, int i, float bs, int bi) {
 // ---------------------------------------------------------------------------
 // staging plan: warp 0 sizes and stages the next chunk of aperture entries.
 
+// staging layouts of the fast form (one 16-byte entry per window sample k)
+constexpr int LAY_QUAD = 0;   // (s_k, s_k+1, s_k+2, s_k+3)
+constexpr int LAY_SD = 1;     // (s_k, s_k+1 - s_k, s_k+1, s_k+2 - s_k+1)
+constexpr int LAY_P2 = 2;     // (s_k, s_k+2, s_k+1, s_k+3)
+
 struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
-  int inrange[kMaxChunk];  // 1 when every item of the pass is in range on this trace
   float scale[kMaxChunk];  // fast form: per-trace scale of the 16-bit store
+  int raw[kMaxChunk];      // fast form: start of the entry's raw window (samples):
+                           // its buffer offset + 8 x its rank in aperture order
   int n;                   // entries in this chunk
+  int n_in;                // fast form: entries on which every item of the pass is in
+                           // range, in slots [0, n_in); the others fill slots
+                           // [kMaxChunk - (n - n_in), kMaxChunk).  Plain form: n_in = n
+  int consumed;            // aperture traces the chunk covers (entries + skipped)
   int bytes;               // bytes staged (TMA form)
 };
 
 constexpr size_t kMetaBytes = ((sizeof(ChunkMeta) + 127) / 128) * 128;
+
+// Slot of the i-th entry (0 <= i < n) of a chunk: the in-range entries first, then
+// the others from the top of the table.
+__device__ __forceinline__ int entry_slot(const ChunkMeta* m, int i) {
+  return i < m->n_in ? i : kMaxChunk - m->n + i;
+}
 
 // Shared-memory layout of the search kernel (bytes), shared by host and device:
 //   [0, 64)   two mbarriers and control words
@@ -223,7 +239,8 @@ __host__ __device__ inline SmemLayout smem_layout(int form, int rc, int cap, int
 
 // Sample window [lo, hi] of one trace that items of a pass can read, for t0 in
 // [T_lo, T_hi] (seconds) and parameters within the pass bounds.  Returns false
-// when no item can be in range.
+// when no item can be in range: then the trace is left out of the chunk, which is
+// exact, because an out-of-range trace only counts in err = N_ap - M.
 template <int METHOD>
 __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_lo, float T_hi, float idt,
                                              int tau, int ns, int& lo, int& hi, bool& inrange) {
@@ -257,6 +274,9 @@ __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_
   smax = fminf(smax, (float)ns + 8.f);
   // in range for sure: tau <= it <= ns - tau - 2 for every item, with one sample of slack
   inrange = t2min > 0.f && smin >= (float)(tau + 1) && smax <= (float)(ns - tau - 3);
+  // out of range for sure (t < tau or t >= ns - tau - 1 for every item, again with a
+  // sample of slack): the trace adds nothing but its out-of-range count
+  if (smax < (float)(tau - 1) || smin > (float)(ns - tau)) return false;
   lo = (int)smin - tau - kMargin;
   hi = (int)smax + tau + 1 + kMargin;
   lo = max(lo, 0);
@@ -267,58 +287,78 @@ __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_
 // Warp 0: choose the entries of the next chunk starting at ap_pos and record, per
 // entry, its geometry, its buffer offset (minus the window start, so that an item
 // indexes with it - tau directly) and its source window (trace, first sample,
-// length, offset) in `src`.  Windows are aligned to ALIGN samples: 4 for FP32 bulk
-// copies (16 bytes), 8 for the fast form's 8-sample staging groups.  Buffer units:
-// floats (plain) or one 16-byte entry per sample (fast).
+// length, offset) in `src`.  Aperture traces on which no item can be in range are
+// consumed without an entry.  meta->n counts entries, meta->consumed the aperture
+// traces the chunk covers.  Fast form: entries on which every item is in range go
+// to the front slots, the others to the back (entry_slot).  Windows are aligned to ALIGN samples: 4 for FP32 bulk
+// copies (16 bytes), 8 for the fast form's raw windows.  Buffer units: floats
+// (plain) or one 16-byte entry per sample (fast).
 template <int METHOD, int FORM>
 __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, int64_t ap_end, float T_lo,
                            float T_hi, ChunkMeta* meta, int4* src) {
   const int lane = threadIdx.x & 31;
   constexpr int ALIGN = (FORM == FORM_PLAIN) ? 4 : 8;
-  int base = 0;
-  int n = 0;
-  for (int round = 0; round < kMaxChunk / 32; ++round) {
-    int64_t k = ap_pos + n + lane;
-    bool have = k < ap_end;
+  int base = 0;       // buffer units used
+  int n_in = 0;       // entries in the in-range part (front)
+  int n_out = 0;      // other entries (back)
+  int consumed = 0;   // aperture traces covered
+  while (n_in + n_out + 32 <= kMaxChunk) {
+    const int64_t k = ap_pos + consumed + lane;
+    const bool have = k < ap_end;
     float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
     int lo = 0, hi = -1;
     int len = 0;
-    bool inr = false;
+    bool inr = false, keep = false;
     int tr = 0;
     float sc = 1.0f;
     if (have) {
       g = P.ap_geo[k];
-      tr = P.ap_tr[k];
-      if (FORM == FORM_FAST && P.storage != STORE_F32) sc = __ldg(P.scale + tr);
-      if (trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi, inr)) {
+      keep = trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi, inr);
+      if (keep) {
+        tr = P.ap_tr[k];
+        if (FORM == FORM_FAST && P.storage != STORE_F32) sc = __ldg(P.scale + tr);
         lo &= ~(ALIGN - 1);
         hi |= (ALIGN - 1);
         len = hi - lo + 1;
       }
     }
-    // inclusive scan of the window lengths over the warp
+    // inclusive scan of the kept windows' lengths over the warp
     int incl = len;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int v = __shfl_up_sync(0xffffffffu, incl, o);
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += v;
     }
-    const bool fits = have && (base + incl <= P.cap);
-    const int nfit = __popc(__ballot_sync(0xffffffffu, fits));   // fits holds for a prefix of lanes
-    if (fits) {
+    // the first kept trace that does not fit ends the chunk
+    const unsigned over = __ballot_sync(0xffffffffu, keep && base + incl > P.cap);
+    const int stop = over ? __ffs(over) - 1 : 32;
+    // the plain form keeps every entry in aperture order at the front
+    const bool take = keep && lane < stop;
+    const bool front = FORM == FORM_PLAIN || inr;
+    const unsigned fr = __ballot_sync(0xffffffffu, take && front);
+    const unsigned bk = __ballot_sync(0xffffffffu, take && !front);
+    if (take) {
+      const unsigned below = (1u << lane) - 1u;
+      const int e = front ? n_in + __popc(fr & below) : kMaxChunk - 1 - (n_out + __popc(bk & below));
       const int off = base + incl - len;
+      const int rank = n_in + n_out + __popc((fr | bk) & below);   // in aperture order
       g.w = __int_as_float(off - lo);
-      meta->geo[n + lane] = g;
-      meta->inrange[n + lane] = (FORM == FORM_FAST && inr) ? 1 : 0;
-      meta->scale[n + lane] = sc;
-      src[n + lane] = make_int4(tr, lo, len, off);
+      meta->geo[e] = g;
+      meta->scale[e] = sc;
+      meta->raw[e] = off + 8 * rank;
+      src[e] = make_int4(tr, lo, len, off);
     }
-    base += nfit > 0 ? __shfl_sync(0xffffffffu, incl, nfit - 1) : 0;
-    n += nfit;
-    if (nfit < 32) break;
+    const int nhave = __popc(__ballot_sync(0xffffffffu, have));
+    base += stop > 0 ? __shfl_sync(0xffffffffu, incl, stop - 1) : 0;
+    n_in += __popc(fr);
+    n_out += __popc(bk);
+    consumed += min(stop, nhave);
+    if (stop < 32 || nhave < 32) break;
   }
   if (lane == 0) {
-    meta->n = n;
+    meta->n = n_in + n_out;
+    meta->n_in = n_in;
+    meta->consumed = consumed;
     meta->bytes = base * 4;
   }
   __syncwarp();
@@ -333,53 +373,56 @@ __device__ __forceinline__ void issue_chunk_copies(const KParams& P, ChunkMeta* 
   if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)meta->bytes);
   __syncwarp();
   const int n = meta->n;
-  for (int e = lane; e < n; e += 32) {
-    const int4 si = src[e];
+  for (int i = lane; i < n; i += 32) {
+    const int4 si = src[entry_slot(meta, i)];
     if (si.z > 0) bulk_g2s(buf + si.w, P.samples + (int64_t)si.x * P.pitch + si.y, (uint32_t)si.z * 4u, bar);
   }
 }
 
 // Fast form, warp 0 after plan_chunk: start one bulk copy (TMA) per staged window
 // of the raw store into `raw`, each window plus the 8 samples after it (the quads
-// of the last samples read 3 past the window).  Entry e lands at raw offset
-// off_e + 8e samples.  The barrier is told the total bytes first.
+// of the last samples read 3 past the window).  The k-th entry in aperture order
+// lands at raw offset off + 8k samples (meta->raw), so windows never overlap.  The barrier is told the total bytes first.
 __device__ __forceinline__ void issue_raw(const KParams& P, const ChunkMeta* meta, const int4* src,
                                           unsigned char* raw, uint64_t* bar) {
   const int lane = threadIdx.x & 31;
   const int n = meta->n;
   const uint32_t unit = P.storage == STORE_F32 ? 4u : 2u;
   uint32_t bytes = 0;
-  for (int e = lane; e < n; e += 32) {
-    const int4 si = src[e];
+  for (int i = lane; i < n; i += 32) {
+    const int4 si = src[entry_slot(meta, i)];
     if (si.z > 0) bytes += (uint32_t)(si.z + 8) * unit;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
   if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
   __syncwarp();
-  for (int e = lane; e < n; e += 32) {
+  for (int i = lane; i < n; i += 32) {
+    const int e = entry_slot(meta, i);
     const int4 si = src[e];
     if (si.z <= 0) continue;
     const int64_t at = (int64_t)si.x * P.pitch + si.y;
     const void* g = P.storage == STORE_F32 ? (const void*)(P.samples + at) : (const void*)(P.samples16 + at);
-    bulk_g2s(raw + (size_t)(si.w + 8 * e) * unit, g, (uint32_t)(si.z + 8) * unit, bar);
+    bulk_g2s(raw + (size_t)meta->raw[e] * unit, g, (uint32_t)(si.z + 8) * unit, bar);
   }
 }
 
 // Fast form, all warps: turn the landed raw windows into 16-byte entries, one per
-// sample k: (s_k, s_k+1, s_k+2, s_k+3) ("quads"), or with SD (s_k, s_k+1 - s_k,
-// s_k+1, s_k+2 - s_k+1) ("value/difference pairs").  Lane l builds entry k0 + l, so
+// sample k: (s_k, s_k+1, s_k+2, s_k+3) ("quads", LAY_QUAD), (s_k, s_k+1 - s_k,
+// s_k+1, s_k+2 - s_k+1) ("value/difference pairs", LAY_SD) or (s_k, s_k+2, s_k+1,
+// s_k+3) ("packed pairs", LAY_P2).  Lane l builds entry k0 + l, so
 // the warp's 16-byte stores cover consecutive addresses (no bank conflicts).
-template <bool SD>
+template <int LAY>
 __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta* meta, const int4* src,
                                               const unsigned char* raw, float4* bufq) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int n = meta->n;
-  for (int e = warp; e < n; e += nwarps) {
+  for (int i = warp; i < n; i += nwarps) {
+    const int e = entry_slot(meta, i);
     const int4 si = src[e];   // (trace, lo, len, off)
     if (si.z <= 0) continue;
     float4* dst = bufq + si.w;
-    const int roff = si.w + 8 * e;
+    const int roff = meta->raw[e];
     const float sc = P.storage == STORE_F32 ? 1.0f : meta->scale[e];
     const float* r32 = reinterpret_cast<const float*>(raw) + roff;
     const uint16_t* r16 = reinterpret_cast<const uint16_t*>(raw) + roff;
@@ -387,7 +430,7 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
     for (int k = lane; k < si.z; k += 32) {
       float v[4];
 #pragma unroll
-      for (int u = 0; u < (SD ? 3 : 4); ++u) {
+      for (int u = 0; u < (LAY == LAY_SD ? 3 : 4); ++u) {
         if (P.storage == STORE_F32) {
           v[u] = r32[k + u];
         } else {
@@ -395,7 +438,9 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
           v[u] = (f16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
         }
       }
-      dst[k] = SD ? make_float4(v[0], v[1] - v[0], v[1], v[2] - v[1]) : make_float4(v[0], v[1], v[2], v[3]);
+      dst[k] = LAY == LAY_SD   ? make_float4(v[0], v[1] - v[0], v[1], v[2] - v[1])
+               : LAY == LAY_P2 ? make_float4(v[0], v[2], v[1], v[3])
+                               : make_float4(v[0], v[1], v[2], v[3]);
     }
   }
 }
@@ -451,11 +496,137 @@ struct PlainAcc {
   int M;
 };
 
-template <int W>
+// Fast form: sums of one item.  den_c is the energy of the current chunk; the
+// Kahan-compensated total and its compensation live in shared memory
+// (kahan_hi/lo).  add(a, x) folds in the window at entry address a with
+// interpolation weight x, in the staging layout LAY.
+template <int W, int LAY>
 struct FastAcc {
   float num[W];
-  float den_c;      // energy of the current chunk; the Kahan-compensated total
-  int M;            // and its compensation live in shared memory (kahan_hi/lo)
+  float den_c;
+  int M;
+
+  __device__ __forceinline__ void reset() {
+#pragma unroll
+    for (int j = 0; j < W; ++j) num[j] = 0.f;
+    den_c = 0.f;
+    M = 0;
+  }
+  __device__ __forceinline__ void add(uint32_t a, float x) {
+    if constexpr (LAY == LAY_SD) {
+      // entries (s_k, d_k, s_k+1, d_k+1): v_j = s_j + x * d_j
+#pragma unroll
+      for (int p = 0; p < W / 2; ++p) {
+        const float4 ev = lds128(a + 32u * p);
+        const float v0 = fmaf(ev.y, x, ev.x);
+        const float v1 = fmaf(ev.w, x, ev.z);
+        num[2 * p] += v0;
+        num[2 * p + 1] += v1;
+        den_c = fmaf(v0, v0, den_c);
+        den_c = fmaf(v1, v1, den_c);
+      }
+      if (W & 1) {
+        const float2 ev = lds64(a + 16u * (W - 1));
+        const float v = fmaf(ev.y, x, ev.x);
+        num[W - 1] += v;
+        den_c = fmaf(v, v, den_c);
+      }
+    } else {
+      float sv[W + 1];
+      load_window<W>(a, sv);
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
+        num[j] += v;
+        den_c = fmaf(v, v, den_c);
+      }
+    }
+  }
+  __device__ __forceinline__ float take_energy() {
+    const float e = den_c;
+    den_c = 0.f;
+    return e;
+  }
+  __device__ __forceinline__ void sums(float& acsq, float& lin) const {
+    acsq = 0.f;
+    lin = 0.f;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      acsq = fmaf(num[j], num[j], acsq);
+      lin += num[j];
+    }
+  }
+};
+
+// Packed layout: entry k = (s_k, s_k+2, s_k+1, s_k+3), so that window samples j
+// and j+2 of an item are one FP32x2 operation: (v_j, v_j+2) = lo + x * (hi - lo)
+// with lo = (s_j, s_j+2), hi = (s_j+1, s_j+3).  Window samples 4q..4q+3 use
+// entries k+4q (pairs (4q, 4q+2)) and k+4q+2 (pairs (4q+1, 4q+3)); the one
+// sample left over (W is odd) is done in scalar arithmetic.
+template <int W>
+struct FastAcc<W, LAY_P2> {
+  static constexpr int NP = (W - 1) / 2 > 0 ? (W - 1) / 2 : 1;
+  float2 np[NP];   // packed sums (num_j, num_j+2)
+  float ns;        // sum of the unpaired window sample
+  float2 den2;     // energy of the current chunk, two partial sums
+  int M;
+
+  __device__ __forceinline__ void reset() {
+#pragma unroll
+    for (int i = 0; i < NP; ++i) np[i] = make_float2(0.f, 0.f);
+    ns = 0.f;
+    den2 = make_float2(0.f, 0.f);
+    M = 0;
+  }
+  __device__ __forceinline__ void pair(int i, float2 lo, float2 hi, float2 xx) {
+    const float2 d = __ffma2_rn(lo, make_float2(-1.f, -1.f), hi);   // hi - lo, exact as a subtraction
+    const float2 v = __ffma2_rn(d, xx, lo);
+    np[i] = __fadd2_rn(np[i], v);
+    den2 = __ffma2_rn(v, v, den2);
+  }
+  __device__ __forceinline__ void single(float s0, float s1, float x) {
+    const float v = fmaf(s1 - s0, x, s0);
+    ns += v;
+    den2.x = fmaf(v, v, den2.x);
+  }
+  __device__ __forceinline__ void add(uint32_t a, float x) {
+    const float2 xx = make_float2(x, x);
+    float4 B = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; 4 * q < W; ++q) {
+      const int j0 = 4 * q;
+      if (j0 + 1 == W && q > 0) {
+        // last sample j0 = W-1: s_j0 and s_j0+1 are in the previous group's entry k+j0-2
+        single(B.y, B.w, x);
+        break;
+      }
+      const float4 A = lds128(a + 64u * q);   // (s_j0, s_j0+2, s_j0+1, s_j0+3)
+      if (j0 + 2 < W) pair(2 * q, make_float2(A.x, A.y), make_float2(A.z, A.w), xx);
+      if (j0 + 3 < W) {
+        B = lds128(a + 64u * q + 32u);        // (s_j0+2, s_j0+4, s_j0+3, s_j0+5)
+        pair(2 * q + 1, make_float2(A.z, A.w), make_float2(B.x, B.y), xx);
+      } else if (j0 + 3 == W) {
+        single(A.z, A.y, x);                  // sample j0+1: s_j0+1, s_j0+2
+      } else if (j0 + 1 == W) {
+        single(A.x, A.z, x);                  // W = 1
+      }
+    }
+  }
+  __device__ __forceinline__ float take_energy() {
+    const float e = den2.x + den2.y;
+    den2 = make_float2(0.f, 0.f);
+    return e;
+  }
+  __device__ __forceinline__ void sums(float& acsq, float& lin) const {
+    acsq = fmaf(ns, ns, 0.f);
+    lin = ns;
+#pragma unroll
+    for (int i = 0; i < (W - 1) / 2; ++i) {
+      acsq = fmaf(np[i].x, np[i].x, acsq);
+      acsq = fmaf(np[i].y, np[i].y, acsq);
+      lin += np[i].x + np[i].y;
+    }
+  }
 };
 
 
@@ -463,7 +634,7 @@ struct FastAcc {
 // ---------------------------------------------------------------------------
 // The search kernel.
 
-template <int METHOD, int FORM, int W, int RC, int MINB, bool SD, bool BRUN, int NT>
+template <int METHOD, int FORM, int W, int RC, int MINB, int LAY, bool BRUN, int NT>
 __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage, NT);
@@ -549,6 +720,11 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
     const float T2sec = __fmul_rn(Tsec, Tsec);                 // CMP: _t0 * _t0
     const float Tsmp = (float)t0;                              // fast form: sample units
     const float T2smp = Tsmp * Tsmp;
+    const float2 Tsmp2 = make_float2(Tsmp, Tsmp);
+    const float2 T2smp2 = make_float2(T2smp, T2smp);
+    const float2 kTwo23x2 = make_float2(8388608.0f, 8388608.0f);
+    const float2 kMinusTwo23x2 = make_float2(-8388608.0f, -8388608.0f);
+    const float2 kMinusOne2 = make_float2(-1.0f, -1.0f);
     const float tau_lo = (float)P.tau;
     const float tau_hi = (float)(P.ns - P.tau - 1);
     const unsigned span = (unsigned)(P.ns - 2 * P.tau - 2);   // valid iff 0 <= it - tau <= span
@@ -556,30 +732,38 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
     for (int pass = 0; pass < P.npass; ++pass) {
       const float* pb = P.pass_bounds + pass * 8;
       const float4* cand = P.cand + pass * P.cpp + warp * RC;
-      float ca[RC], cb[RC], cc[RC];
+      // the thread's RC candidates as pairs (items r, r+1) for the packed FP32x2
+      // traveltimes; an odd RC repeats its last candidate in the unused half
+      constexpr int RP = (RC + 1) / 2;
+      float2 ca2[RP], cb2[RP], cc2[RP];
 #pragma unroll
-      for (int r = 0; r < RC; ++r) {
-        const float4 cv = cand[r];
-        ca[r] = cv.x;
-        cb[r] = cv.y;
-        cc[r] = cv.z;
-      }
-      PlainAcc<W> pa[FORM == FORM_PLAIN ? RC : 1];
-      FastAcc<W> fa[FORM == FORM_FAST ? RC : 1];
-#pragma unroll
-      for (int r = 0; r < RC; ++r) {
-#pragma unroll
-        for (int j = 0; j < W; ++j) {
-          if (FORM == FORM_PLAIN) pa[r].num[j] = 0.f;
-          else fa[r].num[j] = 0.f;
+      for (int r = 0; r < 2 * RP; ++r) {
+        const float4 cv = cand[min(r, RC - 1)];
+        if (r & 1) {
+          ca2[r >> 1].y = cv.x;
+          cb2[r >> 1].y = cv.y;
+          cc2[r >> 1].y = cv.z;
+        } else {
+          ca2[r >> 1].x = cv.x;
+          cb2[r >> 1].x = cv.y;
+          cc2[r >> 1].x = cv.z;
         }
+      }
+      auto CA = [&](int r) { return (r & 1) ? ca2[r >> 1].y : ca2[r >> 1].x; };
+      auto CB = [&](int r) { return (r & 1) ? cb2[r >> 1].y : cb2[r >> 1].x; };
+      auto CC = [&](int r) { return (r & 1) ? cc2[r >> 1].y : cc2[r >> 1].x; };
+      PlainAcc<W> pa[FORM == FORM_PLAIN ? RC : 1];
+      FastAcc<W, LAY> fa[FORM == FORM_FAST ? RC : 1];
+#pragma unroll
+      for (int r = 0; r < RC; ++r) {
         if (FORM == FORM_PLAIN) {
+#pragma unroll
+          for (int j = 0; j < W; ++j) pa[r].num[j] = 0.f;
           pa[r].den = 0.f;
           pa[r].lin = 0.f;
           pa[r].M = 0;
         } else {
-          fa[r].den_c = 0.f;
-          fa[r].M = 0;
+          fa[r].reset();
           kahan_hi[r * NT + threadIdx.x] = 0.f;
           kahan_lo[r * NT + threadIdx.x] = 0.f;
         }
@@ -588,129 +772,119 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
       // compute on a staged chunk (meta, n); the fast form then folds the chunk's
       // energy into the Kahan totals
       auto compute_chunk = [&](const ChunkMeta* meta, const int n) {
+        if (FORM == FORM_PLAIN) {
           for (int e = 0; e < n; ++e) {
             const float4 g = meta->geo[e];
             const int soff = __float_as_int(g.w);
-            if (FORM == FORM_PLAIN) {
-#pragma unroll
-              for (int r = 0; r < RC; ++r) {
-                float t;
-                if (METHOD == METHOD_CMP) {
-                  t = __fmul_rn(__fsqrt_rn(__fadd_rn(T2sec, __fmul_rn(cc[r], g.z))), P.idt);
-                } else {
-                  t = __fadd_rn(Tsec, __fmul_rn(ca[r], g.x));
-                  t = __fadd_rn(__fadd_rn(__fmul_rn(t, t), __fmul_rn(cb[r], g.y)), __fmul_rn(cc[r], g.z));
-                  t = (t < 0.0f) ? -1.0f : __fsqrt_rn(t);
-                  t = __fmul_rn(t, P.idt);
-                }
-                const bool ok = (t >= tau_lo) && (t < tau_hi);
-                const float y = __fadd_rz(t, 8388608.0f);
-                const int it = __float_as_int(y) - 0x4B000000;
-                const float x = ok ? __fsub_rn(t, __fsub_rn(y, 8388608.0f)) : 0.0f;
-                const unsigned idx = min(ok ? (unsigned)(soff + it - P.tau) : (unsigned)P.cap, (unsigned)P.cap);
-                const float* s = buf + idx;
-                float s1 = s[0];
-#pragma unroll
-                for (int j = 0; j < W; ++j) {
-                  const float s0 = s1;
-                  s1 = s[j + 1];
-                  const float v = __fadd_rn(__fmul_rn(__fsub_rn(s1, s0), x), s0);
-                  pa[r].num[j] = __fadd_rn(pa[r].num[j], v);
-                  pa[r].den = __fadd_rn(pa[r].den, __fmul_rn(v, v));
-                  pa[r].lin = __fadd_rn(pa[r].lin, v);
-                }
-                pa[r].M += ok ? 1 : 0;
-              }
-            } else {
-              // t2 in samples^2 for item r on this trace
-              // B-run candidates share A and C: (t0 + A|dm|)^2 + C h once per trace
-              float q0 = 0.f;
-              if (BRUN && METHOD == METHOD_CRS) {
-                const float u0 = fmaf(ca[0], g.x, Tsmp);
-                q0 = fmaf(u0, u0, cc[0] * g.z);
-              }
-              auto t2_of = [&](int r) {
-                if (METHOD == METHOD_CMP) return fmaf(cc[r], g.z, T2smp);
-                if (BRUN) return fmaf(cb[r], g.y, q0);
-                const float u = fmaf(ca[r], g.x, Tsmp);
-                return fmaf(u, u, fmaf(cb[r], g.y, cc[r] * g.z));
-              };
-              auto accumulate = [&](int r, uint32_t a, float x) {
-                if (SD) {
-                  // entries (s_k, d_k, s_k+1, d_k+1): v_j = s_j + x * d_j
-#pragma unroll
-                  for (int p = 0; p < W / 2; ++p) {
-                    const float4 ev = lds128(a + 32u * p);
-                    const float v0 = fmaf(ev.y, x, ev.x);
-                    const float v1 = fmaf(ev.w, x, ev.z);
-                    fa[r].num[2 * p] += v0;
-                    fa[r].num[2 * p + 1] += v1;
-                    fa[r].den_c = fmaf(v0, v0, fa[r].den_c);
-                    fa[r].den_c = fmaf(v1, v1, fa[r].den_c);
-                  }
-                  if (W & 1) {
-                    const float2 ev = lds64(a + 16u * (W - 1));
-                    const float v = fmaf(ev.y, x, ev.x);
-                    fa[r].num[W - 1] += v;
-                    fa[r].den_c = fmaf(v, v, fa[r].den_c);
-                  }
-                } else {
-                  float sv[W + 1];
-                  load_window<W>(a, sv);
-#pragma unroll
-                  for (int j = 0; j < W; ++j) {
-                    const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
-                    fa[r].num[j] += v;
-                    fa[r].den_c = fmaf(v, v, fa[r].den_c);
-                  }
-                }
-              };
-              if (meta->inrange[e]) {
-                // every item in range: address = bits(t + 2^23) * 16 + base (mod 2^32),
-                // clamped to the buffer as a guard
-                const uint32_t base = bufq_addr + 16u * (uint32_t)(soff - P.tau) - 16u * 0x4B000000u;
-                const uint32_t top = bufq_addr + 16u * (uint32_t)P.cap;
-#pragma unroll
-                for (int r = 0; r < RC; ++r) {
-                  const float t = sqrt_fast(t2_of(r));
-                  const float y = __fadd_rz(t, 8388608.0f);
-                  accumulate(r, min(__float_as_uint(y) * 16u + base, top), t - (y - 8388608.0f));
-                }
-              } else {
-#pragma unroll
-                for (int r = 0; r < RC; ++r) {
-                  const float t = sqrt_fast(t2_of(r));   // NaN for t2 < 0: out of range below
-                  const float y = __fadd_rz(t, 8388608.0f);
-                  const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
-                  const bool ok = (unsigned)rel <= span;
-                  const float x = ok ? t - (y - 8388608.0f) : 0.0f;
-                  const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
-                  accumulate(r, bufq_addr + 16u * idx, x);
-                  fa[r].M += ok ? 1 : 0;
-                }
-              }
-            }
-          }
-          if (FORM == FORM_FAST) {
-            // traces flagged in range count for every item
-            int ninr = 0;
-            for (int e = 0; e < n; ++e) ninr += meta->inrange[e];
-#pragma unroll
-            for (int r = 0; r < RC; ++r) fa[r].M += ninr;
-          }
-          if (FORM == FORM_FAST) {
 #pragma unroll
             for (int r = 0; r < RC; ++r) {
-              // Kahan: fold this chunk's energy into the compensated total
-              const int o = r * NT + threadIdx.x;
-              const float hi = kahan_hi[o], lo = kahan_lo[o];
-              const float yv = fa[r].den_c - lo;
-              const float tv = hi + yv;
-              kahan_lo[o] = (tv - hi) - yv;
-              kahan_hi[o] = tv;
-              fa[r].den_c = 0.f;
+              float t;
+              if (METHOD == METHOD_CMP) {
+                t = __fmul_rn(__fsqrt_rn(__fadd_rn(T2sec, __fmul_rn(CC(r), g.z))), P.idt);
+              } else {
+                t = __fadd_rn(Tsec, __fmul_rn(CA(r), g.x));
+                t = __fadd_rn(__fadd_rn(__fmul_rn(t, t), __fmul_rn(CB(r), g.y)), __fmul_rn(CC(r), g.z));
+                t = (t < 0.0f) ? -1.0f : __fsqrt_rn(t);
+                t = __fmul_rn(t, P.idt);
+              }
+              const bool ok = (t >= tau_lo) && (t < tau_hi);
+              const float y = __fadd_rz(t, 8388608.0f);
+              const int it = __float_as_int(y) - 0x4B000000;
+              const float x = ok ? __fsub_rn(t, __fsub_rn(y, 8388608.0f)) : 0.0f;
+              const unsigned idx = min(ok ? (unsigned)(soff + it - P.tau) : (unsigned)P.cap, (unsigned)P.cap);
+              const float* s = buf + idx;
+              float s1 = s[0];
+#pragma unroll
+              for (int j = 0; j < W; ++j) {
+                const float s0 = s1;
+                s1 = s[j + 1];
+                const float v = __fadd_rn(__fmul_rn(__fsub_rn(s1, s0), x), s0);
+                pa[r].num[j] = __fadd_rn(pa[r].num[j], v);
+                pa[r].den = __fadd_rn(pa[r].den, __fmul_rn(v, v));
+                pa[r].lin = __fadd_rn(pa[r].lin, v);
+              }
+              pa[r].M += ok ? 1 : 0;
             }
           }
+        } else {
+          const int n_in = meta->n_in;
+          const uint32_t top = bufq_addr + 16u * (uint32_t)P.cap;
+          // traces on which every item is in range: traveltimes of item pairs in
+          // FP32x2, address = bits(t + 2^23) * 16 + base (mod 2^32), clamped to the
+          // buffer as a guard
+          for (int e = 0; e < n_in; ++e) {
+            const float4 g = meta->geo[e];
+            const uint32_t base = bufq_addr + 16u * (uint32_t)(__float_as_int(g.w) - P.tau) - 16u * 0x4B000000u;
+            const float2 gx2 = make_float2(g.x, g.x), gy2 = make_float2(g.y, g.y), gz2 = make_float2(g.z, g.z);
+            // B-run candidates share A and C: (t0 + A|dm|)^2 + C h once per trace
+            float2 q02 = make_float2(0.f, 0.f);
+            if (BRUN && METHOD == METHOD_CRS) {
+              const float u0 = fmaf(CA(0), g.x, Tsmp);
+              const float q0 = fmaf(u0, u0, CC(0) * g.z);
+              q02 = make_float2(q0, q0);
+            }
+#pragma unroll
+            for (int rp = 0; rp < RP; ++rp) {
+              float2 t2;
+              if (METHOD == METHOD_CMP) {
+                t2 = __ffma2_rn(cc2[rp], gz2, T2smp2);
+              } else if (BRUN) {
+                t2 = __ffma2_rn(cb2[rp], gy2, q02);
+              } else {
+                const float2 u = __ffma2_rn(ca2[rp], gx2, Tsmp2);
+                t2 = __ffma2_rn(u, u, __ffma2_rn(cb2[rp], gy2, __fmul2_rn(cc2[rp], gz2)));
+              }
+              const float2 t = make_float2(sqrt_fast(t2.x), sqrt_fast(t2.y));
+              const float2 y = __fadd2_rz(t, kTwo23x2);
+              const float2 x = __ffma2_rn(__fadd2_rn(y, kMinusTwo23x2), kMinusOne2, t);   // t - floor(t)
+              fa[2 * rp].add(min(__float_as_uint(y.x) * 16u + base, top), x.x);
+              if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * 16u + base, top), x.y);
+            }
+          }
+          // the other traces: per-item range checks; an out-of-range item reads the
+          // zero block with weight 0 and does not count
+          for (int e = kMaxChunk - (n - n_in); e < kMaxChunk; ++e) {
+            const float4 g = meta->geo[e];
+            const int soff = __float_as_int(g.w);
+            float q0 = 0.f;
+            if (BRUN && METHOD == METHOD_CRS) {
+              const float u0 = fmaf(CA(0), g.x, Tsmp);
+              q0 = fmaf(u0, u0, CC(0) * g.z);
+            }
+#pragma unroll
+            for (int r = 0; r < RC; ++r) {
+              float t2;
+              if (METHOD == METHOD_CMP) {
+                t2 = fmaf(CC(r), g.z, T2smp);
+              } else if (BRUN) {
+                t2 = fmaf(CB(r), g.y, q0);
+              } else {
+                const float u = fmaf(CA(r), g.x, Tsmp);
+                t2 = fmaf(u, u, fmaf(CB(r), g.y, CC(r) * g.z));
+              }
+              const float t = sqrt_fast(t2);   // NaN for t2 < 0: out of range below
+              const float y = __fadd_rz(t, 8388608.0f);
+              const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
+              const bool ok = (unsigned)rel <= span;
+              const float x = ok ? t - (y - 8388608.0f) : 0.0f;
+              const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
+              fa[r].add(bufq_addr + 16u * idx, x);
+              fa[r].M += ok ? 1 : 0;
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < RC; ++r) {
+            // in-range traces count for every item
+            fa[r].M += n_in;
+            // Kahan: fold this chunk's energy into the compensated total
+            const int o = r * NT + threadIdx.x;
+            const float hi = kahan_hi[o], lo = kahan_lo[o];
+            const float yv = fa[r].take_energy() - lo;
+            const float tv = hi + yv;
+            kahan_lo[o] = (tv - hi) - yv;
+            kahan_hi[o] = tv;
+          }
+        }
       };
 
       if (FORM == FORM_PLAIN) {
@@ -729,8 +903,9 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
             if (threadIdx.x == 0) atomicOr(P.status, ST_TIMEOUT);
             return;
           }
+          const int consumed = meta->consumed;
           compute_chunk(meta, n);
-          ap_pos += n;
+          ap_pos += consumed;
           __syncthreads();   // buffer and meta free for the next chunk
         }
       } else {
@@ -750,12 +925,12 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
           // rides on the barrier after the conversion
           const bool ok = wait_bar(bars + cur, (phases >> cur) & 1u);
           phases ^= 1u << cur;
-          if (ok) convert_chunk<SD>(P, mc, srcs + cur * kMaxChunk, raw_at(cur), bufq);
+          if (ok) convert_chunk<LAY>(P, mc, srcs + cur * kMaxChunk, raw_at(cur), bufq);
           if (__syncthreads_or(!ok)) {   // entries ready; raw buffer cur free
             if (threadIdx.x == 0) atomicOr(P.status, ST_TIMEOUT);
             return;
           }
-          const int64_t next = ap_pos + n;
+          const int64_t next = ap_pos + mc->consumed;
           if (warp == 0) {
             ChunkMeta* mn = meta_at(cur ^ 1);
             if (next < ap_end) {
@@ -784,12 +959,8 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
           sem = ok ? __fdiv_rn(acsq, __fmul_rn(pa[r].den, mf)) : kSent;
           stk = ok ? __fdiv_rn(pa[r].lin, __fmul_rn((float)W, mf)) : kSent;
         } else {
-          float acsq = 0.f, lin = 0.f;
-#pragma unroll
-          for (int j = 0; j < W; ++j) {
-            acsq = fmaf(fa[r].num[j], fa[r].num[j], acsq);
-            lin += fa[r].num[j];
-          }
+          float acsq, lin;
+          fa[r].sums(acsq, lin);
           const float den = kahan_hi[r * NT + threadIdx.x] - kahan_lo[r * NT + threadIdx.x];
           const float mf = (float)fa[r].M;
           const int err = napert - fa[r].M;

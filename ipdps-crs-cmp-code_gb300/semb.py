@@ -28,6 +28,8 @@ CMP, CRS = 0, 1
 PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
+ABI_VERSION = 2
+MAX_VARIANTS = 12   # SEMB_MAX_VARIANTS
 
 OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODEV = range(10)
 
@@ -123,6 +125,8 @@ def lib():
         f = getattr(L, name)
         f.restype = res
         f.argtypes = args
+    if L.semb_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{LIB_PATH} has ABI {L.semb_abi_version()}, this binding expects {ABI_VERSION}: rebuild")
     _lib = L
     return L
 
@@ -286,7 +290,7 @@ class Plan:
         """Pick the fastest search-kernel variant on a sample of this plan's tasks.
         Returns (chosen variant, [sample ms per variant, -1 when absent])."""
         v = C.c_int32()
-        ms = (C.c_double * 8)()
+        ms = (C.c_double * MAX_VARIANTS)()
         _check(lib().semb_plan_autotune(self._h, C.byref(v), ms), "semb_plan_autotune")
         return int(v.value), [float(x) for x in ms]
 
