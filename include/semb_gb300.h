@@ -32,7 +32,7 @@ extern "C" {
 #define SEMB_ABI_VERSION 2
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
-#define SEMB_MAX_VARIANTS 12
+#define SEMB_MAX_VARIANTS 16
 
 /* Methods. */
 enum { SEMB_CMP = 0, SEMB_CRS = 1 };

@@ -17,13 +17,14 @@ static SearchEntry lookup(int method, int form, int w, int v) {
   return form == FORM_PLAIN ? search_entry_crs_plain(w, v) : search_entry_crs_fast(w, v);
 }
 
-int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt) {
+int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt, int* pipe) {
   if (v < 0 || v >= kMaxVariants) return 0;
   SearchEntry e = lookup(method, form, w, v);
   *rc = e.rc;
   *minb = e.minb;
   *brun = e.brun;
   *nt = e.nt;
+  if (pipe) *pipe = e.pipe;
   return e.fn != nullptr;
 }
 

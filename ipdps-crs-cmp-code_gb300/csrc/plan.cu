@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.h"
+#include "pipe_kernel.cuh"
 #include "plan_kernels.cuh"
 #include "semb_kernels.cuh"
 
@@ -26,7 +27,7 @@ namespace semb {
 // Launchers of the search kernel instantiations (kernels_*.cu).
 int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
-int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt);
+int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt, int* pipe);
 constexpr int kVariantSlots = SEMB_MAX_VARIANTS;
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
@@ -239,8 +240,8 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
 int configure_variant(semb_plan* pl, int v) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  int rc = 0, minb = 0, brun = 0, nt = 0;
-  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt))
+  int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0;
+  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe))
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
   const int ncand = pl->ncand;
   // search order; a negative slot -1-g marks padding that repeats candidate g.
@@ -256,10 +257,16 @@ int configure_variant(semb_plan* pl, int v) {
     slots = pl->order;
   }
   const int nslots = (int)slots.size();
+  // the most warps whose padding stays within 1% of the slots, else the least padding
   int best_nw = nt / 32, best_tot = INT32_MAX;
   for (int nw = nt / 32; nw >= 4; --nw) {
     const int per = nw * rc;
     const int tot = ((nslots + per - 1) / per) * per;
+    if ((int64_t)tot * 100 <= (int64_t)nslots * 101) {
+      best_tot = tot;
+      best_nw = nw;
+      break;
+    }
     if (tot < best_tot) {
       best_tot = tot;
       best_nw = nw;
@@ -312,9 +319,12 @@ int configure_variant(semb_plan* pl, int v) {
   const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
   const size_t budget = (227 * 1024) / minb - 1024;
   int cap = form == FORM_PLAIN ? 32768 : 8192;
-  while (cap > 64 && smem_layout(form, rc, cap, store, nt).total > budget) cap -= 64;
+  auto smem_of = [&](int cp) {
+    return pipe ? pipe_layout(rc, cp, store, nt).total : smem_layout(form, rc, cp, store, nt).total;
+  };
+  while (cap > 64 && smem_of(cap) > budget) cap -= 64;
   if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
-  const size_t smem = smem_layout(form, rc, cap, store, nt).total;
+  const size_t smem = smem_of(cap);
   if (smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", pl->ns);
   int occ = 0;
   SEMB_TRY(search_occupancy(p.method, form, pl->w, v, best_nw, smem, &occ));
@@ -823,7 +833,7 @@ int semb_plan_set_variant(semb_plan* pl, int32_t variant) {
   SEMB_CUDA(cudaSetDevice(pl->device));
   const int form = pl->p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
   int rc = 0, minb = 0, brun = 0, nt = 0;
-  if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun, &nt))
+  if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun, &nt, nullptr))
     return fail(SEMB_E_ARG, "no search kernel variant %d for this plan", variant);
   return configure_variant(pl, variant);
 }
@@ -852,7 +862,7 @@ int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
   for (int v = 0; v < kVariantSlots; ++v) {
     int rc = 0, minb = 0, brun = 0, nt = 0;
     if (ms_of_variant) ms_of_variant[v] = -1.0;
-    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt)) continue;
+    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, nullptr)) continue;
     SEMB_TRY(configure_variant(pl, v));
     KParams P = make_kparams(pl);
     P.tasks = d_sample;

@@ -9,12 +9,15 @@
 // keeps the fastest; variant 0 is the default.  The value/difference staging
 // layout (LAY_SD) saves one FP32 op per window sample for 50% more shared-memory
 // bytes per evaluation; the packed layout (LAY_P2) does two window samples per
-// FP32x2 instruction.  RC values keep the per-item
+// FP32x2 instruction.  Variants 11 and up use the pipelined kernel
+// (semb_pipe_kernel), whose warps hand chunks over through mbarriers instead of
+// meeting at CTA barriers.  RC values keep the per-item
 // register state within 65536 / (256 * MINB) registers without spilling
 // (checked with -Xptxas -v).
 #pragma once
 
 #include "common.h"
+#include "pipe_kernel.cuh"
 #include "semb_kernels.cuh"
 
 namespace semb {
@@ -25,13 +28,19 @@ struct SearchEntry {
   int minb;
   int brun;   // candidates laid out as B runs of RC (CRS)
   int nt;     // threads per CTA
+  int pipe;   // 1: semb_pipe_kernel (decoupled staging ring), 0: semb_search_kernel
 };
 
 constexpr int kMaxVariants = SEMB_MAX_VARIANTS;
 
 template <int METHOD, int FORM, int W, int RC, int MINB, int LAY = LAY_QUAD, bool BRUN = false, int NT = 256>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 0};
+}
+
+template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256>
+SearchEntry pipe_entry() {
+  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 1};
 }
 
 // Plain form: one variant per window.
@@ -44,7 +53,7 @@ SearchEntry plain_entry() {
 template <int METHOD, int FORM>
 SearchEntry search_entry(int w, int variant) {
   if constexpr (FORM == FORM_PLAIN) {
-    if (variant != 0) return {nullptr, 0, 0, 0, 0};
+    if (variant != 0) return {nullptr, 0, 0, 0, 0, 0};
     switch (w) {
       case 1: return plain_entry<METHOD, 1>();
       case 3: return plain_entry<METHOD, 3>();
@@ -56,7 +65,7 @@ SearchEntry search_entry(int w, int variant) {
       case 13: return plain_entry<METHOD, 13>();
       case 15: return plain_entry<METHOD, 15>();
 #endif
-      default: return {nullptr, 0, 0, 0, 0};
+      default: return {nullptr, 0, 0, 0, 0, 0};
     }
   } else {
   // fast form
@@ -67,6 +76,8 @@ SearchEntry search_entry(int w, int variant) {
       if (METHOD == METHOD_CRS && variant == 4) return entry<METHOD, FORM, 1, 7, 2, LAY_QUAD, true>();
       if (METHOD == METHOD_CRS && variant == 5) return entry<METHOD, FORM, 1, 8, 2, LAY_QUAD, true>();
       if (variant == 6) return entry<METHOD, FORM, 1, 8, 4, LAY_QUAD, false, 128>();
+      if (variant == 11) return pipe_entry<METHOD, 1, 8, 2, LAY_QUAD>();
+      if (variant == 12) return pipe_entry<METHOD, 1, 8, 1, LAY_QUAD, false, 512>();
       break;
     case 3:
       if (variant == 0) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -80,6 +91,11 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 8) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2>();
       if (variant == 9) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_P2, METHOD == METHOD_CRS, 128>();
       if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 3, 8, 2, LAY_P2, true>();
+      if (variant == 11) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
+      if (variant == 12) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 1, LAY_P2, false, 512>();
+      if (variant == 13) return pipe_entry<METHOD, 3, 6, 2, LAY_QUAD>();
+      if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 3, 7, 1, LAY_P2, true, 512>();
+      if (variant == 15) return pipe_entry<METHOD, 3, 12, 1, LAY_P2, false, 384>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -92,6 +108,9 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 8) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2>();
       if (variant == 9) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_P2, METHOD == METHOD_CRS, 128>();
       if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 5, 8, 2, LAY_P2, true>();
+      if (variant == 11) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
+      if (variant == 12) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 6), 1, LAY_P2, false, 512>();
+      if (variant == 15) return pipe_entry<METHOD, 5, 10, 1, LAY_P2, false, 384>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;
@@ -102,7 +121,7 @@ SearchEntry search_entry(int w, int variant) {
 #endif
     default: break;
   }
-  return {nullptr, 0, 0, 0, 0};
+  return {nullptr, 0, 0, 0, 0, 0};
   }
 }
 

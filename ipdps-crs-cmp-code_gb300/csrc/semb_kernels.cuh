@@ -414,8 +414,9 @@ __device__ __forceinline__ void issue_raw(const KParams& P, const ChunkMeta* met
 // the warp's 16-byte stores cover consecutive addresses (no bank conflicts).
 template <int LAY>
 __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta* meta, const int4* src,
-                                              const unsigned char* raw, float4* bufq) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+                                              const unsigned char* raw, float4* bufq, int first_warp = 0) {
+  const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int warp = ((threadIdx.x >> 5) + nwarps - first_warp) % nwarps;   // rank from first_warp on
   const int n = meta->n;
   for (int i = warp; i < n; i += nwarps) {
     const int e = entry_slot(meta, i);

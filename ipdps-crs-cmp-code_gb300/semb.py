@@ -29,7 +29,7 @@ PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
 ABI_VERSION = 2
-MAX_VARIANTS = 12   # SEMB_MAX_VARIANTS
+MAX_VARIANTS = 16   # SEMB_MAX_VARIANTS
 
 OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODEV = range(10)
 

@@ -149,7 +149,7 @@ def test_reupload_and_rerun_are_stable():
         assert np.array_equal(x, y)
 
 
-@pytest.mark.parametrize("case", ["cmp_line", "crs_line", "crs_uneven_w5"])
+@pytest.mark.parametrize("case", ["cmp_line", "cmp_uneven_w1", "cmp_farout", "crs_line", "crs_uneven_w5"])
 def test_every_variant_agrees_with_the_default(case):
     """Each search-kernel variant (items per thread, CTAs per SM, staging and
     candidate layouts) gives the default variant's picks and semblances."""
