@@ -78,6 +78,7 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 6) return entry<METHOD, FORM, 1, 8, 4, LAY_QUAD, false, 128>();
       if (variant == 11) return pipe_entry<METHOD, 1, 8, 2, LAY_QUAD>();
       if (variant == 12) return pipe_entry<METHOD, 1, 8, 1, LAY_QUAD, false, 512>();
+      if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 1, 7, 1, LAY_QUAD, true, 512>();
       break;
     case 3:
       if (variant == 0) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -93,9 +94,9 @@ SearchEntry search_entry(int w, int variant) {
       if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 3, 8, 2, LAY_P2, true>();
       if (variant == 11) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 12) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 1, LAY_P2, false, 512>();
-      if (variant == 13) return pipe_entry<METHOD, 3, 6, 2, LAY_QUAD>();
+      if (variant == 13) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_SD, METHOD == METHOD_CRS, 512>();
       if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 3, 7, 1, LAY_P2, true, 512>();
-      if (variant == 15) return pipe_entry<METHOD, 3, 12, 1, LAY_P2, false, 384>();
+      if (variant == 15) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -110,7 +111,9 @@ SearchEntry search_entry(int w, int variant) {
       if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 5, 8, 2, LAY_P2, true>();
       if (variant == 11) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 12) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 6), 1, LAY_P2, false, 512>();
-      if (variant == 15) return pipe_entry<METHOD, 5, 10, 1, LAY_P2, false, 384>();
+      if (variant == 13) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_SD, METHOD == METHOD_CRS, 512>();
+      if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 5, 7, 1, LAY_P2, true, 512>();
+      if (variant == 15) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;
