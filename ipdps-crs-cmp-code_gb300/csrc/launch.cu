@@ -17,7 +17,7 @@ static SearchEntry lookup(int method, int form, int w, int v) {
   return form == FORM_PLAIN ? search_entry_crs_plain(w, v) : search_entry_crs_fast(w, v);
 }
 
-int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt, int* pipe) {
+int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt, int* pipe, int* lay) {
   if (v < 0 || v >= kMaxVariants) return 0;
   SearchEntry e = lookup(method, form, w, v);
   *rc = e.rc;
@@ -25,7 +25,16 @@ int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* 
   *brun = e.brun;
   *nt = e.nt;
   if (pipe) *pipe = e.pipe;
+  if (lay) *lay = e.lay;
   return e.fn != nullptr;
+}
+
+// Variant a plan starts with (before any autotuning): for CRS the pipelined
+// 512-thread B-run kernel, the fastest on the CRS workloads measured on GB300;
+// for CMP the two-barrier kernel's variant 0.
+int default_variant(int method, int form, int w) {
+  if (method == METHOD_CRS && form == FORM_FAST && w <= 5) return 14;
+  return 0;
 }
 
 int search_occupancy(int method, int form, int w, int v, int nwarps, size_t smem, int* ctas_per_sm) {

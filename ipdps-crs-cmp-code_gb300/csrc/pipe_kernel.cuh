@@ -71,7 +71,7 @@ struct PipeLayout {
   size_t prod, meta, tag, src, tops, kahan, quad, quad_stride, raw, raw_stride, total;
 };
 
-__host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, int nt) {
+__host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, int nt, int lay) {
   PipeLayout L;
   L.prod = 128;
   L.meta = L.prod + align128(sizeof(Producer));
@@ -80,7 +80,7 @@ __host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, 
   L.tops = L.src + (size_t)kMetaRing * kMaxChunk * 16;
   L.kahan = L.tops + align128(3 * (size_t)kTopK * nt * 4);
   L.quad = L.kahan + align128(2 * (size_t)rc * nt * 4);
-  L.quad_stride = align128(((size_t)cap + kZeroSlots) * 16);
+  L.quad_stride = align128(((size_t)cap + kZeroSlots) * lay_entry_bytes(lay));
   L.raw = L.quad + kStages * L.quad_stride;
   L.raw_stride = align128(((size_t)cap + 8 * kMaxChunk) * (storage == STORE_F32 ? 4 : 2));
   L.total = L.raw + kRawBufs * L.raw_stride;
@@ -94,7 +94,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT>
 __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT);
+  const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT, LAY);
+  constexpr uint32_t EB = lay_entry_bytes(LAY);   // bytes per staged entry
   uint64_t* raw_full = reinterpret_cast<uint64_t*>(smem_raw);   // [kRawBufs]
   uint64_t* q_full = raw_full + kRawBufs;                        // [kStages]
   uint64_t* q_empty = q_full + kStages;                          // [kStages]
@@ -123,7 +124,8 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   constexpr float kSent = (METHOD == METHOD_CMP) ? -1.0f : 0.0f;
 
   for (int s = 0; s < kStages; ++s)
-    if (threadIdx.x < kZeroSlots) quad_at(s)[P.cap + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (threadIdx.x < kZeroSlots * (EB / 16))
+      quad_at(s)[P.cap * (EB / 16) + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (threadIdx.x == 0) {
     for (int b = 0; b < kRawBufs; ++b) mbar_init(&raw_full[b], 1);
     for (int s = 0; s < kStages; ++s) {
@@ -302,15 +304,15 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
     {
       const int n = meta->n, n_in = meta->n_in;
       const uint32_t bufq_addr = smem_u32(quad_at(c));
-      const uint32_t top = bufq_addr + 16u * (uint32_t)P.cap;
+      const uint32_t top = bufq_addr + EB * (uint32_t)P.cap;
       const float2 Tsmp2 = make_float2(Tsmp, Tsmp);
       const float2 T2smp2 = make_float2(T2smp, T2smp);
       // traces on which every item is in range: traveltimes of item pairs in
-      // FP32x2, address = bits(t + 2^23) * 16 + base (mod 2^32), clamped to the
+      // FP32x2, address = bits(t + 2^23) * EB + base (mod 2^32), clamped to the
       // stage as a guard
       for (int e = 0; e < n_in; ++e) {
         const float4 g = meta->geo[e];
-        const uint32_t base = bufq_addr + 16u * (uint32_t)(__float_as_int(g.w) - P.tau) - 16u * 0x4B000000u;
+        const uint32_t base = bufq_addr + EB * (uint32_t)(__float_as_int(g.w) - P.tau) - EB * 0x4B000000u;
         const float2 gx2 = make_float2(g.x, g.x), gy2 = make_float2(g.y, g.y), gz2 = make_float2(g.z, g.z);
         float2 q02 = make_float2(0.f, 0.f);
         if (BRUN && METHOD == METHOD_CRS) {
@@ -333,8 +335,8 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
           const float2 t = make_float2(sqrt_fast(t2.x), sqrt_fast(t2.y));
           const float2 y = __fadd2_rz(t, kTwo23x2);
           const float2 x = __ffma2_rn(__fadd2_rn(y, kMinusTwo23x2), kMinusOne2, t);   // t - floor(t)
-          fa[2 * rp].add(min(__float_as_uint(y.x) * 16u + base, top), x.x);
-          if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * 16u + base, top), x.y);
+          fa[2 * rp].add(min(__float_as_uint(y.x) * EB + base, top), x.x);
+          if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * EB + base, top), x.y);
         }
       }
       // the other traces: per-item range checks; an out-of-range item reads the
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
           const bool ok = (unsigned)rel <= span;
           const float x = ok ? t - (y - 8388608.0f) : 0.0f;
           const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
-          fa[r].add(bufq_addr + 16u * idx, x);
+          fa[r].add(bufq_addr + EB * idx, x);
           fa[r].M += ok ? 1 : 0;
         }
       }

@@ -27,9 +27,11 @@ namespace semb {
 // Launchers of the search kernel instantiations (kernels_*.cu).
 int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
-int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt, int* pipe);
+int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt, int* pipe,
+                   int* lay);
 constexpr int kVariantSlots = SEMB_MAX_VARIANTS;
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
+int default_variant(int method, int form, int w);
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);
 
@@ -240,8 +242,8 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
 int configure_variant(semb_plan* pl, int v) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0;
-  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe))
+  int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0, lay = 0;
+  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe, &lay))
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
   const int ncand = pl->ncand;
   // search order; a negative slot -1-g marks padding that repeats candidate g.
@@ -274,6 +276,23 @@ int configure_variant(semb_plan* pl, int v) {
   }
   const int cpp = best_nw * rc;
   const int npass = (nslots + cpp - 1) / cpp;
+
+  // staging capacity, shared memory and residency, checked before the plan's
+  // device state changes (a variant that does not fit leaves the plan as it was)
+  const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
+  const size_t budget = (227 * 1024) / minb - 1024;
+  int cap = form == FORM_PLAIN ? 32768 : 8192;
+  auto smem_of = [&](int cp) {
+    return pipe ? pipe_layout(rc, cp, store, nt, lay).total : smem_layout(form, rc, cp, store, nt).total;
+  };
+  while (cap > 64 && smem_of(cap) > budget) cap -= 64;
+  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
+  const size_t smem = smem_of(cap);
+  if (smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", pl->ns);
+  int occ = 0;
+  SEMB_TRY(search_occupancy(p.method, form, pl->w, v, best_nw, smem, &occ));
+  if (occ <= 0) return fail(SEMB_E_CUDA, "search kernel cannot be resident with %zu bytes", smem);
+
   const int npad = npass * cpp;
   std::vector<float4> cand(npad);
   std::vector<float> bounds((size_t)npass * 8, 0.f);
@@ -316,19 +335,6 @@ int configure_variant(semb_plan* pl, int v) {
   SEMB_CUDA(cudaMemcpyAsync(pl->d_pass_bounds, bounds.data(), bounds.size() * 4, cudaMemcpyHostToDevice,
                             pl->stream));
 
-  const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
-  const size_t budget = (227 * 1024) / minb - 1024;
-  int cap = form == FORM_PLAIN ? 32768 : 8192;
-  auto smem_of = [&](int cp) {
-    return pipe ? pipe_layout(rc, cp, store, nt).total : smem_layout(form, rc, cp, store, nt).total;
-  };
-  while (cap > 64 && smem_of(cap) > budget) cap -= 64;
-  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
-  const size_t smem = smem_of(cap);
-  if (smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", pl->ns);
-  int occ = 0;
-  SEMB_TRY(search_occupancy(p.method, form, pl->w, v, best_nw, smem, &occ));
-  if (occ <= 0) return fail(SEMB_E_CUDA, "search kernel cannot be resident with %zu bytes", smem);
   SEMB_CUDA(cudaStreamSynchronize(pl->stream));
   pl->variant = v;
   pl->rc = rc;
@@ -616,7 +622,8 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
     SEMB_TRY(dev_alloc(&pl->d_top_stk, nout * kTopK));
   }
 
-  SEMB_TRY(configure_variant(pl, 0));
+  // the default variant of this method and window; variant 0 where it does not fit
+  if (configure_variant(pl, default_variant(p.method, form, pl->w)) != SEMB_OK) SEMB_TRY(configure_variant(pl, 0));
   cudaEventRecord(pl->ev[5], st);
   SEMB_CUDA(cudaStreamSynchronize(st));
   float ms = 0.f;
@@ -833,7 +840,7 @@ int semb_plan_set_variant(semb_plan* pl, int32_t variant) {
   SEMB_CUDA(cudaSetDevice(pl->device));
   const int form = pl->p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
   int rc = 0, minb = 0, brun = 0, nt = 0;
-  if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun, &nt, nullptr))
+  if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun, &nt, nullptr, nullptr))
     return fail(SEMB_E_ARG, "no search kernel variant %d for this plan", variant);
   return configure_variant(pl, variant);
 }
@@ -862,8 +869,9 @@ int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
   for (int v = 0; v < kVariantSlots; ++v) {
     int rc = 0, minb = 0, brun = 0, nt = 0;
     if (ms_of_variant) ms_of_variant[v] = -1.0;
-    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, nullptr)) continue;
-    SEMB_TRY(configure_variant(pl, v));
+    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, nullptr, nullptr)) continue;
+    // a variant whose staging does not fit this plan's traces is skipped
+    if (configure_variant(pl, v) != SEMB_OK) continue;
     KParams P = make_kparams(pl);
     P.tasks = d_sample;
     P.ntasks = S;

@@ -6,7 +6,7 @@
 // give the scheduler more warps to hide barrier and load latency, and smaller
 // CTAs let the others fill the cycles one of them spends at a barrier.  The plan's
 // autotuner times the variants of its window on a sample of its own tasks and
-// keeps the fastest; variant 0 is the default.  The value/difference staging
+// keeps the fastest; default_variant() (launch.cu) is where a plan starts.  The value/difference staging
 // layout (LAY_SD) saves one FP32 op per window sample for 50% more shared-memory
 // bytes per evaluation; the packed layout (LAY_P2) does two window samples per
 // FP32x2 instruction.  Variants 11 and up use the pipelined kernel
@@ -29,18 +29,19 @@ struct SearchEntry {
   int brun;   // candidates laid out as B runs of RC (CRS)
   int nt;     // threads per CTA
   int pipe;   // 1: semb_pipe_kernel (decoupled staging ring), 0: semb_search_kernel
+  int lay;    // staging layout (LAY_*)
 };
 
 constexpr int kMaxVariants = SEMB_MAX_VARIANTS;
 
 template <int METHOD, int FORM, int W, int RC, int MINB, int LAY = LAY_QUAD, bool BRUN = false, int NT = 256>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 0};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 0, LAY};
 }
 
 template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256>
 SearchEntry pipe_entry() {
-  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 1};
+  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 1, LAY};
 }
 
 // Plain form: one variant per window.
@@ -53,7 +54,7 @@ SearchEntry plain_entry() {
 template <int METHOD, int FORM>
 SearchEntry search_entry(int w, int variant) {
   if constexpr (FORM == FORM_PLAIN) {
-    if (variant != 0) return {nullptr, 0, 0, 0, 0, 0};
+    if (variant != 0) return {nullptr, 0, 0, 0, 0, 0, 0};
     switch (w) {
       case 1: return plain_entry<METHOD, 1>();
       case 3: return plain_entry<METHOD, 3>();
@@ -65,7 +66,7 @@ SearchEntry search_entry(int w, int variant) {
       case 13: return plain_entry<METHOD, 13>();
       case 15: return plain_entry<METHOD, 15>();
 #endif
-      default: return {nullptr, 0, 0, 0, 0, 0};
+      default: return {nullptr, 0, 0, 0, 0, 0, 0};
     }
   } else {
   // fast form
@@ -124,7 +125,7 @@ SearchEntry search_entry(int w, int variant) {
 #endif
     default: break;
   }
-  return {nullptr, 0, 0, 0, 0, 0};
+  return {nullptr, 0, 0, 0, 0, 0, 0};
   }
 }
 

@@ -178,6 +178,9 @@ constexpr int LAY_QUAD = 0;   // (s_k, s_k+1, s_k+2, s_k+3)
 constexpr int LAY_SD = 1;     // (s_k, s_k+1 - s_k, s_k+1, s_k+2 - s_k+1)
 constexpr int LAY_P2 = 2;     // (s_k, s_k+2, s_k+1, s_k+3)
 
+// bytes of one staged entry
+__host__ __device__ constexpr int lay_entry_bytes(int) { return 16; }
+
 struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
   float scale[kMaxChunk];  // fast form: per-trace scale of the 16-bit store
@@ -422,7 +425,7 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
     const int e = entry_slot(meta, i);
     const int4 si = src[e];   // (trace, lo, len, off)
     if (si.z <= 0) continue;
-    float4* dst = bufq + si.w;
+    float4* dst = bufq + (size_t)si.w * (lay_entry_bytes(LAY) / 16);
     const int roff = meta->raw[e];
     const float sc = P.storage == STORE_F32 ? 1.0f : meta->scale[e];
     const float* r32 = reinterpret_cast<const float*>(raw) + roff;
@@ -629,6 +632,7 @@ struct FastAcc<W, LAY_P2> {
     }
   }
 };
+
 
 
 
