@@ -152,13 +152,27 @@ def timed_runs(plan: semb.Plan, warmup: int, steps: int):
     return dev_ms, search_ms, wall, plan.stats()
 
 
-def traffic_from_profiles(workload: str):
+def traffic_from_profiles(workload: str, ncdps: int, trace_evals: int):
+    """DRAM bytes per search launch from the single-pass ncu captures summarised in
+    profiles/traffic.json: the captured figure when the workload and CDP count match,
+    else that capture scaled by trace-evaluations (the staged windows and the top-4
+    outputs grow with the CDPs searched).  None when no capture covers the workload."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(workload)
+            table = json.load(f)
     except (OSError, ValueError):
         return None
+    e = table.get(workload)
+    if e is None:
+        return None
+    src = table.get(e["scaled_from"]) if "scaled_from" in e else e
+    if not src or "dram_read" not in src:
+        return None
+    captured = src["dram_read"] + src["dram_write"]
+    if "scaled_from" not in e and src["ncdps"] == ncdps:
+        return float(captured)
+    return float(captured) * trace_evals / src["trace_evals"]
 
 
 def oracle_mod():
@@ -353,9 +367,22 @@ def run_ours(args, rank, world, dist):
 
     peak = semb.probe_fp32_tflops(dev)
     achieved = flops / (ms_search * 1e-3) / 1e12
-    traffic = traffic_from_profiles(args.workload)
+    traffic = traffic_from_profiles(args.workload, st["ncdps"], st["trace_evals"])
+    hbm = None
+    if traffic is not None:
+        # HBM side of the roofline: DRAM bytes per launch over the live launch time,
+        # against the measured copy bandwidth
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                hbm_peak = float(json.load(f)["hbm_gbs"])
+        except (OSError, ValueError, KeyError):
+            hbm_peak = None
+        got = traffic / (ms_search * 1e-3) / 1e9
+        hbm = {"achieved_gbs": got, "peak_gbs": hbm_peak, "frac": got / hbm_peak if hbm_peak else None,
+               "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)"}
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "traffic": traffic, "peak_source": "measured live: semb_probe_fp32 FMA throughput",
+            "traffic": traffic, "traffic_unit": "DRAM bytes per search launch (ncu)", "hbm": hbm,
+            "peak_source": "measured live: semb_probe_fp32 FMA throughput",
             "flops_per_launch": flops, "launch_ms": ms_search}
     clocks = clk.summary()
     line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
