@@ -280,6 +280,7 @@ def run_ours(args, rank, world, dist):
     plan = semb.Plan(semb.params(method, mode=semb.BATCHED, storage=storage, **s.params), device=dev)
     plan.upload(arrays.view())
     tune = plan.autotune() if args.tune else None
+    buckets = plan.buckets()
     st0 = plan.stats()
     nap = int(round(st0["trace_evals"] / (st0["ns"] * st0["ncand"])))
     # per-kernel split (search vs re-pick) from direct launches
@@ -398,7 +399,8 @@ def run_ours(args, rank, world, dist):
             "speedup_batched_vs_plain": res["plain"]["ms"] / (total_ms / args.steps),
             "roofline": roof, "clocks": clocks, "gpu_launches": int(st["kernel_launches"]) * args.steps,
             "autotune": {"variant": st["variant"], "sample_ms": tune[1] if tune else None,
-                         "ctas_per_sm": st["ctas_per_sm"]}}
+                         "ctas_per_sm": st["ctas_per_sm"],
+                         "buckets": [dict(zip(("ap_lo", "ap_hi", "tasks", "variant"), b)) for b in buckets]}}
     for k in ("store_bf16", "store_f32"):
         if k in res:
             line[k] = res[k]

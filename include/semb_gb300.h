@@ -29,10 +29,13 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 2
+#define SEMB_ABI_VERSION 3
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
 #define SEMB_MAX_VARIANTS 16
+
+/* Aperture buckets of a batched plan's work queue (semb_plan_buckets). */
+#define SEMB_MAX_BUCKETS 4
 
 /* Methods. */
 enum { SEMB_CMP = 0, SEMB_CRS = 1 };
@@ -231,6 +234,17 @@ int semb_plan_stats(const semb_plan* plan, semb_stats* out);
  * No counterpart in the reference, which has one fixed launch shape
  * (CRS/CUDA/src/main.cu:45-51, 439). */
 int semb_plan_autotune(semb_plan* plan, int32_t* chosen, double* ms_of_variant);
+
+/* The aperture buckets of the plan's work queue: a batched plan splits its CDPs,
+ * sorted by aperture size, at 1024, 384 and 128 aperture traces (merging buckets
+ * too small to fill the GPU), and searches each bucket with its own launch and its
+ * own kernel variant; semb_plan_autotune tunes each bucket on a sample of its own
+ * tasks and merges neighbours that chose the same variant.  The plain form has one
+ * bucket.  Arrays have SEMB_MAX_BUCKETS entries (any may be NULL): aperture range
+ * [ap_lo, ap_hi], tasks (CDP x 32-sample t0 blocks) and variant of each bucket.
+ * No counterpart in the reference. */
+int semb_plan_buckets(const semb_plan* plan, int32_t* nbuckets, int32_t* ap_lo, int32_t* ap_hi,
+                      int32_t* ntasks, int32_t* variant);
 
 /* Use search-kernel variant `variant` (0..SEMB_MAX_VARIANTS-1) for later runs; SEMB_E_ARG when this
  * plan's window and form have no such variant.  No counterpart in the reference. */

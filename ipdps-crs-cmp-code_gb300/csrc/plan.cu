@@ -30,6 +30,12 @@ int launch_search(int method, int form, int w, int variant, const KParams& P, in
 int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt, int* pipe,
                    int* lay);
 constexpr int kVariantSlots = SEMB_MAX_VARIANTS;
+constexpr int kMaxBuckets = SEMB_MAX_BUCKETS;
+// aperture split points of the work queue (traces): buckets > 1024, 385-1024,
+// 129-384 and <= 128 aperture traces
+constexpr int kBucketSplits = 3;
+constexpr int kBucketAp[kBucketSplits] = {1024, 384, 128};
+static_assert(kBucketSplits + 1 <= kMaxBuckets, "bucket table");
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int default_variant(int method, int form, int w);
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
@@ -38,6 +44,28 @@ int launch_repick(int w, const RepickParams& R, cudaStream_t st);
 }  // namespace semb
 
 using namespace semb;
+
+namespace {
+
+// One search-kernel configuration: a variant with its candidate table, per-pass
+// parameter bounds, staging capacity, shared memory and residency.
+struct KernelCfg {
+  int variant = -1, rc = 0, minb = 0, nwarps = 0, cpp = 0, npass = 0, cap = 0, occ = 0;
+  size_t smem = 0;
+  float4* d_cand = nullptr;
+  float* d_pass_bounds = nullptr;
+};
+
+// A contiguous range of the aperture-sorted work queue, searched by one launch
+// with its own configuration.
+struct Bucket {
+  int begin = 0, end = 0;     // tasks [begin, end)
+  int ap_lo = 0, ap_hi = 0;   // aperture traces of its CDPs
+  int64_t work = 0;           // sum of aperture traces over its tasks
+  KernelCfg cfg;
+};
+
+}  // namespace
 
 struct semb_plan {
   semb_params p{};
@@ -51,14 +79,10 @@ struct semb_plan {
   float dt = 0.f, idt = 0.f;
   double dt64 = 0.0, idt64 = 0.0;
   int tau = 0, w = 1;
-  int ncand = 0, npass = 0, cpp = 0, nwarps = 0, rc = 0;
+  int ncand = 0;
   int ntasks = 0, max_ap = 0;
-  size_t smem = 0;
-  int cap = 0;
-  int grid = 0, ctas_per_sm = 0;
   int64_t n_nbr = 0;
   float cand0_a = 0.f, cand0_b = 0.f, cand0_c = 0.f;
-  int variant = 0, minb = 2;
   // candidate grid kept on the host for re-configuration
   std::vector<float> ga, gb, gc;
   std::vector<double> g64;
@@ -74,11 +98,11 @@ struct semb_plan {
   Geo64* d_ap_geo64 = nullptr;
   int64_t* d_nbr_off = nullptr;
   int32_t* d_nbr = nullptr;
-  float4* d_cand = nullptr;
-  float* d_pass_bounds = nullptr;
   double* d_cand64 = nullptr;
   int2* d_tasks = nullptr;
-  int* d_counter = nullptr;
+  int* d_counter = nullptr;   // work-queue heads, one per bucket
+  // aperture buckets of the work queue (batched form; one bucket in the plain form)
+  std::vector<Bucket> buckets;
   int32_t* d_ctr = nullptr;
   float* d_str = nullptr;
   float* d_stk = nullptr;
@@ -127,6 +151,17 @@ void dev_free(T*& p) {
   p = nullptr;
 }
 
+void free_cfg(KernelCfg& c) {
+  dev_free(c.d_cand);
+  dev_free(c.d_pass_bounds);
+  c.variant = -1;
+}
+
+void drop_graph(semb_plan* pl) {
+  if (pl->graph) cudaGraphExecDestroy(pl->graph);
+  pl->graph = nullptr;
+}
+
 void free_data(semb_plan* pl) {
   dev_free(pl->d_samples);
   dev_free(pl->d_samples16);
@@ -137,8 +172,8 @@ void free_data(semb_plan* pl) {
   dev_free(pl->d_ap_geo64);
   dev_free(pl->d_nbr_off);
   dev_free(pl->d_nbr);
-  dev_free(pl->d_cand);
-  dev_free(pl->d_pass_bounds);
+  for (Bucket& b : pl->buckets) free_cfg(b.cfg);
+  pl->buckets.clear();
   dev_free(pl->d_cand64);
   dev_free(pl->d_tasks);
   dev_free(pl->d_ctr);
@@ -234,12 +269,12 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
   }
 }
 
-// Launch configuration of search-kernel variant v: candidates per pass (warps x
-// RC, warps chosen to waste the least padding), the search-order candidate
-// table padded to whole passes, per-pass parameter bounds, the staging capacity
-// (as large as the variant's resident CTAs per SM allow, never less than one
-// whole trace), shared memory, occupancy and grid.
-int configure_variant(semb_plan* pl, int v) {
+// Launch configuration of search-kernel variant v into `out`: candidates per pass
+// (warps x RC), the search-order candidate table padded to whole passes, per-pass
+// parameter bounds, the staging capacity (as large as the variant's resident CTAs
+// per SM allow, never less than one whole trace), shared memory and occupancy.
+// Whether the variant fits is checked before `out` changes.
+int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
   int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0, lay = 0;
@@ -327,32 +362,59 @@ int configure_variant(semb_plan* pl, int v) {
       bp[5] = std::max(bp[5], pl->gc[gi]);
     }
   }
-  dev_free(pl->d_cand);
-  dev_free(pl->d_pass_bounds);
-  SEMB_TRY(dev_alloc(&pl->d_cand, npad));
-  SEMB_TRY(dev_alloc(&pl->d_pass_bounds, bounds.size()));
-  SEMB_CUDA(cudaMemcpyAsync(pl->d_cand, cand.data(), npad * sizeof(float4), cudaMemcpyHostToDevice, pl->stream));
-  SEMB_CUDA(cudaMemcpyAsync(pl->d_pass_bounds, bounds.data(), bounds.size() * 4, cudaMemcpyHostToDevice,
-                            pl->stream));
-
-  SEMB_CUDA(cudaStreamSynchronize(pl->stream));
-  pl->variant = v;
-  pl->rc = rc;
-  pl->minb = minb;
-  pl->nwarps = best_nw;
-  pl->cpp = cpp;
-  pl->npass = npass;
-  pl->cap = cap;
-  pl->smem = smem;
-  pl->ctas_per_sm = occ;
-  pl->grid = form == FORM_PLAIN ? pl->ntasks : std::min(pl->ntasks, pl->sms * occ);
-  pl->stats.grid_ctas = pl->grid;
-  pl->stats.ctas_per_sm = occ;
-  pl->stats.variant = v;
-  if (pl->graph) {
-    cudaGraphExecDestroy(pl->graph);
-    pl->graph = nullptr;
+  KernelCfg c;
+  if (dev_alloc(&c.d_cand, npad) != SEMB_OK || dev_alloc(&c.d_pass_bounds, bounds.size()) != SEMB_OK) {
+    free_cfg(c);
+    return fail(SEMB_E_NOMEM, "candidate table of %d entries", npad);
   }
+  cudaError_t e = cudaMemcpyAsync(c.d_cand, cand.data(), npad * sizeof(float4), cudaMemcpyHostToDevice, pl->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c.d_pass_bounds, bounds.data(), bounds.size() * 4, cudaMemcpyHostToDevice, pl->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
+  if (e != cudaSuccess) {
+    free_cfg(c);
+    SEMB_CUDA(e);
+  }
+  c.variant = v;
+  c.rc = rc;
+  c.minb = minb;
+  c.nwarps = best_nw;
+  c.cpp = cpp;
+  c.npass = npass;
+  c.cap = cap;
+  c.smem = smem;
+  c.occ = occ;
+  free_cfg(out);
+  out = c;
+  drop_graph(pl);
+  return SEMB_OK;
+}
+
+int bucket_grid(const semb_plan* pl, const Bucket& b) {
+  const int n = b.end - b.begin;
+  return pl->p.mode == SEMB_PLAIN_F32 ? n : std::min(n, pl->sms * b.cfg.occ);
+}
+
+// The bucket that holds most of the search work (its variant is the one reported).
+const Bucket& main_bucket(const semb_plan* pl) {
+  size_t best = 0;
+  for (size_t i = 1; i < pl->buckets.size(); ++i)
+    if (pl->buckets[i].work > pl->buckets[best].work) best = i;
+  return pl->buckets[best];
+}
+
+void refresh_stats(semb_plan* pl) {
+  const Bucket& b = main_bucket(pl);
+  pl->stats.grid_ctas = bucket_grid(pl, b);
+  pl->stats.ctas_per_sm = b.cfg.occ;
+  pl->stats.variant = b.cfg.variant;
+}
+
+// Variant v for every bucket.  A variant fits all buckets or none (the fit depends
+// on the plan's traces only), so a failure leaves the plan unchanged.
+int set_all(semb_plan* pl, int v) {
+  for (Bucket& b : pl->buckets) SEMB_TRY(build_cfg(pl, v, b.cfg));
+  refresh_stats(pl);
   return SEMB_OK;
 }
 
@@ -397,7 +459,7 @@ int semb_plan_create(const semb_params* p, int32_t device, semb_plan** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking);
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&pl->ev[i]);
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_status, sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&pl->d_counter, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&pl->d_counter, kMaxBuckets * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_repicked, sizeof(unsigned long long));
   if (e != cudaSuccess) {
     semb_plan_destroy(pl);
@@ -609,6 +671,42 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   SEMB_TRY(dev_alloc(&pl->d_tasks, tasks.size()));
   SEMB_CUDA(cudaMemcpyAsync(pl->d_tasks, tasks.data(), tasks.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
 
+  // aperture buckets (batched form): contiguous ranges of the sorted queue split at
+  // kBucketAp traces, each searched by its own launch with its own variant; a
+  // bucket too small to fill the GPU a few times over joins its larger neighbour
+  {
+    auto ap_of = [&](size_t t) { return (int)(ap_off[tasks[t].x + 1] - ap_off[tasks[t].x]); };
+    std::vector<Bucket> bs;
+    size_t t = 0;
+    const size_t nt = tasks.size();
+    const int nsplit = form == FORM_FAST ? kBucketSplits : 0;
+    for (int k = 0; k <= nsplit && t < nt; ++k) {
+      const int lo = k < nsplit ? kBucketAp[k] : INT32_MIN;   // bucket k holds apertures > lo
+      Bucket b;
+      b.begin = (int)t;
+      while (t < nt && ap_of(t) > lo) ++t;
+      if (k == nsplit) t = nt;
+      b.end = (int)t;
+      if (b.end > b.begin) bs.push_back(b);
+    }
+    if (bs.empty()) bs.push_back(Bucket{});
+    for (size_t i = 0; i + 1 < bs.size();) {
+      const int small = std::max(1, pl->sms * 8);
+      if (bs[i].end - bs[i].begin < small || bs[i + 1].end - bs[i + 1].begin < small) {
+        bs[i].end = bs[i + 1].end;
+        bs.erase(bs.begin() + (long)i + 1);
+      } else {
+        ++i;
+      }
+    }
+    for (Bucket& b : bs) {
+      b.ap_hi = b.end > b.begin ? ap_of(b.begin) : 0;
+      b.ap_lo = b.end > b.begin ? ap_of(b.end - 1) : 0;
+      for (int i = b.begin; i < b.end; ++i) b.work += ap_of(i);
+    }
+    pl->buckets = bs;
+  }
+
   // outputs
   const size_t nout = (size_t)g->ncdps * g->ns;
   SEMB_TRY(dev_alloc(&pl->d_ctr, nout));
@@ -623,7 +721,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   }
 
   // the default variant of this method and window; variant 0 where it does not fit
-  if (configure_variant(pl, default_variant(p.method, form, pl->w)) != SEMB_OK) SEMB_TRY(configure_variant(pl, 0));
+  if (set_all(pl, default_variant(p.method, form, pl->w)) != SEMB_OK) SEMB_TRY(set_all(pl, 0));
   cudaEventRecord(pl->ev[5], st);
   SEMB_CUDA(cudaStreamSynchronize(st));
   float ms = 0.f;
@@ -639,9 +737,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   pl->stats.ncand = pl->ncand;
   pl->stats.evals = (int64_t)pl->ncdps * pl->ns * pl->ncand;
   pl->stats.trace_evals = pl->nap * (int64_t)pl->ns * pl->ncand;
-  pl->stats.grid_ctas = pl->grid;
-  pl->stats.ctas_per_sm = pl->ctas_per_sm;
-  pl->stats.variant = pl->variant;
+  refresh_stats(pl);
   pl->stats.sms = pl->sms;
   pl->uploaded = true;
   return SEMB_OK;
@@ -651,7 +747,9 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
 
 namespace {
 
-KParams make_kparams(semb_plan* pl) {
+// Kernel parameters for configuration `cfg` over tasks[0, ntasks) with work-queue
+// head `counter`.
+KParams make_kparams_cfg(semb_plan* pl, const KernelCfg& cfg, const int2* tasks, int ntasks, int* counter) {
   KParams P{};
   P.samples = pl->d_samples;
   P.samples16 = pl->d_samples16;
@@ -661,18 +759,18 @@ KParams make_kparams(semb_plan* pl) {
   P.ap_off = pl->d_ap_off;
   P.ap_tr = pl->d_ap_tr;
   P.ap_geo = pl->d_ap_geo;
-  P.cand = pl->d_cand;
-  P.pass_bounds = pl->d_pass_bounds;
-  P.npass = pl->npass;
-  P.cpp = pl->cpp;
-  P.tasks = pl->d_tasks;
-  P.ntasks = pl->ntasks;
-  P.counter = pl->d_counter;
+  P.cand = cfg.d_cand;
+  P.pass_bounds = cfg.d_pass_bounds;
+  P.npass = cfg.npass;
+  P.cpp = cfg.cpp;
+  P.tasks = tasks;
+  P.ntasks = ntasks;
+  P.counter = counter;
   P.ns = pl->ns;
   P.tau = pl->tau;
   P.dt = pl->dt;
   P.idt = pl->idt;
-  P.cap = pl->cap;
+  P.cap = cfg.cap;
   P.ctr = pl->d_ctr;
   P.str = pl->d_str;
   P.stk = pl->d_stk;
@@ -684,12 +782,17 @@ KParams make_kparams(semb_plan* pl) {
   return P;
 }
 
+KParams make_kparams(semb_plan* pl, int bucket) {
+  const Bucket& b = pl->buckets[bucket];
+  return make_kparams_cfg(pl, b.cfg, pl->d_tasks + b.begin, b.end - b.begin, pl->d_counter + bucket);
+}
+
 // Enqueue one whole search on the plan's stream (no synchronization).
 int enqueue_run(semb_plan* pl, bool timed) {
   cudaStream_t st = pl->stream;
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  KParams P = make_kparams(pl);
+  KParams P = make_kparams(pl, 0);
   int launches = 0;
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[0], st));
   if (pl->ns < 2 * pl->tau + 2) {
@@ -709,10 +812,15 @@ int enqueue_run(semb_plan* pl, bool timed) {
     SEMB_TRY(launch_stt00(pl->w, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
     ++launches;
   }
-  if (form == FORM_FAST) SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st));
+  if (form == FORM_FAST) SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, kMaxBuckets * sizeof(int), st));
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[1], st));
-  SEMB_TRY(launch_search(p.method, form, pl->w, pl->variant, P, pl->nwarps, pl->grid, pl->smem, st));
-  ++launches;
+  for (int i = 0; i < (int)pl->buckets.size(); ++i) {
+    const Bucket& b = pl->buckets[i];
+    if (b.end == b.begin) continue;
+    const KParams Pb = make_kparams(pl, i);
+    SEMB_TRY(launch_search(p.method, form, pl->w, b.cfg.variant, Pb, b.cfg.nwarps, bucket_grid(pl, b), b.cfg.smem, st));
+    ++launches;
+  }
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
   if (form == FORM_FAST) {
     RepickParams R{};
@@ -842,7 +950,7 @@ int semb_plan_set_variant(semb_plan* pl, int32_t variant) {
   int rc = 0, minb = 0, brun = 0, nt = 0;
   if (!search_variant(pl->p.method, form, pl->w, variant, &rc, &minb, &brun, &nt, nullptr, nullptr))
     return fail(SEMB_E_ARG, "no search kernel variant %d for this plan", variant);
-  return configure_variant(pl, variant);
+  return set_all(pl, variant);
 }
 
 int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
@@ -852,50 +960,97 @@ int semb_plan_autotune(semb_plan* pl, int32_t* chosen, double* ms_of_variant) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
   cudaStream_t st = pl->stream;
-  // a strided sample of the (aperture-sorted) task list: big and small apertures
-  const int S = std::min(pl->ntasks, std::max(1, pl->sms * 12));
-  std::vector<int2> all(pl->ntasks), sample(S);
+  std::vector<int2> all(pl->ntasks);
   SEMB_CUDA(cudaMemcpy(all.data(), pl->d_tasks, all.size() * sizeof(int2), cudaMemcpyDeviceToHost));
-  for (int i = 0; i < S; ++i) sample[i] = all[(int64_t)i * pl->ntasks / S];
+  const int smax = std::max(1, pl->sms * 8);
   int2* d_sample = nullptr;
-  SEMB_TRY(dev_alloc(&d_sample, S));
+  SEMB_TRY(dev_alloc(&d_sample, smax));
   struct Free {
     int2* p;
-    ~Free() { cudaFree(p); }
-  } guard{d_sample};
-  SEMB_CUDA(cudaMemcpy(d_sample, sample.data(), S * sizeof(int2), cudaMemcpyHostToDevice));
-  int best = -1;
-  double best_ms = 1e300;
-  for (int v = 0; v < kVariantSlots; ++v) {
-    int rc = 0, minb = 0, brun = 0, nt = 0;
-    if (ms_of_variant) ms_of_variant[v] = -1.0;
-    if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, nullptr, nullptr)) continue;
-    // a variant whose staging does not fit this plan's traces is skipped
-    if (configure_variant(pl, v) != SEMB_OK) continue;
-    KParams P = make_kparams(pl);
-    P.tasks = d_sample;
-    P.ntasks = S;
-    const int grid = form == FORM_PLAIN ? S : std::min(S, pl->sms * pl->ctas_per_sm);
-    float ms = 1e30f;
-    for (int rep = 0; rep < 3; ++rep) {
-      SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st));
-      SEMB_CUDA(cudaEventRecord(pl->ev[4], st));
-      SEMB_TRY(launch_search(p.method, form, pl->w, v, P, pl->nwarps, grid, pl->smem, st));
-      SEMB_CUDA(cudaEventRecord(pl->ev[5], st));
-      SEMB_CUDA(cudaStreamSynchronize(st));
-      float t = 0.f;
-      SEMB_CUDA(cudaEventElapsedTime(&t, pl->ev[4], pl->ev[5]));
-      if (rep > 0) ms = std::min(ms, t);   // the first launch is a warm-up
+    KernelCfg trial;
+    ~Free() {
+      cudaFree(p);
+      free_cfg(trial);
     }
-    if (ms_of_variant) ms_of_variant[v] = ms;
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = v;
+  } guard{d_sample, {}};
+  std::vector<double> total(kVariantSlots, 0.0);
+  std::vector<char> fits(kVariantSlots, 1);
+  for (Bucket& b : pl->buckets) {
+    const int n = b.end - b.begin;
+    if (n == 0) continue;
+    // a strided sample of the bucket's (aperture-sorted) tasks
+    const int S = std::min(n, smax);
+    std::vector<int2> sample(S);
+    for (int i = 0; i < S; ++i) sample[i] = all[b.begin + (int64_t)i * n / S];
+    SEMB_CUDA(cudaMemcpy(d_sample, sample.data(), S * sizeof(int2), cudaMemcpyHostToDevice));
+    int best = -1;
+    double best_ms = 1e300;
+    for (int v = 0; v < kVariantSlots; ++v) {
+      int rc = 0, minb = 0, brun = 0, nt = 0;
+      // a variant with no kernel for this window, or whose staging does not fit
+      // this plan's traces, is skipped
+      if (!fits[v] || !search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, nullptr, nullptr) ||
+          build_cfg(pl, v, guard.trial) != SEMB_OK) {
+        fits[v] = 0;
+        continue;
+      }
+      const KParams P = make_kparams_cfg(pl, guard.trial, d_sample, S, pl->d_counter);
+      const int grid = form == FORM_PLAIN ? S : std::min(S, pl->sms * guard.trial.occ);
+      float ms = 1e30f;
+      for (int rep = 0; rep < 3; ++rep) {
+        SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st));
+        SEMB_CUDA(cudaEventRecord(pl->ev[4], st));
+        SEMB_TRY(launch_search(p.method, form, pl->w, v, P, guard.trial.nwarps, grid, guard.trial.smem, st));
+        SEMB_CUDA(cudaEventRecord(pl->ev[5], st));
+        SEMB_CUDA(cudaStreamSynchronize(st));
+        float t = 0.f;
+        SEMB_CUDA(cudaEventElapsedTime(&t, pl->ev[4], pl->ev[5]));
+        if (rep > 0) ms = std::min(ms, t);   // the first launch is a warm-up
+      }
+      total[v] += ms;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = v;
+      }
+    }
+    if (best < 0) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", pl->w);
+    SEMB_TRY(build_cfg(pl, best, b.cfg));
+  }
+  // neighbouring buckets that chose the same variant become one launch
+  for (size_t i = 0; i + 1 < pl->buckets.size();) {
+    Bucket& a = pl->buckets[i];
+    Bucket& c = pl->buckets[i + 1];
+    if (a.cfg.variant == c.cfg.variant) {
+      a.end = c.end;
+      a.ap_lo = c.ap_lo;
+      a.work += c.work;
+      free_cfg(c.cfg);
+      pl->buckets.erase(pl->buckets.begin() + (long)i + 1);
+    } else {
+      ++i;
     }
   }
-  if (best < 0) return fail(SEMB_E_WINDOW, "no search kernel for w = %d", pl->w);
-  SEMB_TRY(configure_variant(pl, best));
-  if (chosen) *chosen = best;
+  drop_graph(pl);
+  refresh_stats(pl);
+  if (ms_of_variant)
+    for (int v = 0; v < kVariantSlots; ++v) ms_of_variant[v] = fits[v] ? total[v] : -1.0;
+  if (chosen) *chosen = main_bucket(pl).cfg.variant;
+  return SEMB_OK;
+}
+
+int semb_plan_buckets(const semb_plan* pl, int32_t* nbuckets, int32_t* ap_lo, int32_t* ap_hi, int32_t* ntasks,
+                      int32_t* variant) {
+  if (!pl || !nbuckets) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_buckets before semb_plan_upload");
+  const int n = (int)pl->buckets.size();
+  *nbuckets = n;
+  for (int i = 0; i < n; ++i) {
+    const Bucket& b = pl->buckets[i];
+    if (ap_lo) ap_lo[i] = b.ap_lo;
+    if (ap_hi) ap_hi[i] = b.ap_hi;
+    if (ntasks) ntasks[i] = b.end - b.begin;
+    if (variant) variant[i] = b.cfg.variant;
+  }
   return SEMB_OK;
 }
 

@@ -28,15 +28,16 @@ CMP, CRS = 0, 1
 PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_VARIANTS = 16   # SEMB_MAX_VARIANTS
+MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
 OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODEV = range(10)
 
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
-    "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
+    "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
     "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
 
@@ -109,6 +110,7 @@ def lib():
         "semb_plan_stats": (C.c_int, [P, P]),
         "semb_neighbours_noalloc": (C.c_int, [P, P, P, P, P, i32, i32, P, P, i64, P, P]),
         "semb_plan_autotune": (C.c_int, [P, P, P]),
+        "semb_plan_buckets": (C.c_int, [P, P, P, P, P, P]),
         "semb_plan_set_variant": (C.c_int, [P, i32]),
         "semb_plan_use_graph": (C.c_int, [P, i32]),
         "semb_plan_destroy": (C.c_int, [P]),
@@ -293,6 +295,13 @@ class Plan:
         ms = (C.c_double * MAX_VARIANTS)()
         _check(lib().semb_plan_autotune(self._h, C.byref(v), ms), "semb_plan_autotune")
         return int(v.value), [float(x) for x in ms]
+
+    def buckets(self) -> list:
+        """Aperture buckets of the work queue: [(ap_lo, ap_hi, ntasks, variant), ...]."""
+        n = C.c_int32()
+        arrs = [(C.c_int32 * MAX_BUCKETS)() for _ in range(4)]
+        _check(lib().semb_plan_buckets(self._h, C.byref(n), *arrs), "semb_plan_buckets")
+        return [tuple(int(a[i]) for a in arrs) for i in range(n.value)]
 
     def set_variant(self, v: int) -> None:
         _check(lib().semb_plan_set_variant(self._h, int(v)), "semb_plan_set_variant")
