@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 3
+#define SEMB_ABI_VERSION 4
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
 #define SEMB_MAX_VARIANTS 16
@@ -52,6 +52,10 @@ enum { SEMB_CMP = 0, SEMB_CRS = 1 };
 enum { SEMB_PLAIN_F32 = 0, SEMB_BATCHED = 1 };
 enum { SEMB_STORE_F32 = 0, SEMB_STORE_F16 = 1, SEMB_STORE_BF16 = 2 };
 enum { SEMB_REPICK_OFF = 0, SEMB_REPICK_NEAR_TIES = 1, SEMB_REPICK_ALWAYS = 2 };
+/* CRS midpoint displacement.  SEMB_DM_SIGNED has no counterpart in the reference,
+ * whose CRS operator uses the unsigned distance |dm| (CRS/OpenMP/src/main.cpp:198-204):
+ * dm = (mx - mx0) cos(azimuth) + (my - my0) sin(azimuth), dm^2 = dm * dm. */
+enum { SEMB_DM_ABS = 0, SEMB_DM_SIGNED = 1 };
 
 /* Status codes. */
 enum {
@@ -83,11 +87,14 @@ typedef struct semb_params {
   int32_t apm;           /* -apm: midpoint aperture (m), CRS only */
   int32_t storage;       /* SEMB_STORE_*, batched form only */
   double tau;            /* -tau: half window (s) */
-  double azimuth;        /* -azimuth (deg): accepted; the reference's CRS operator
-                            uses the unsigned midpoint distance, which this
-                            search keeps, so it does not change results */
+  double azimuth;        /* -azimuth (deg), counterclockwise from +x.  With
+                            dm_mode SEMB_DM_ABS (the reference's operator, which
+                            never reads it) it has no effect. */
   int32_t repick;        /* SEMB_REPICK_*, batched form only */
   float repick_gap;      /* near-tie threshold on semblance (batched form) */
+  int32_t dm_mode;       /* CRS midpoint displacement: SEMB_DM_ABS (|dm|, as the
+                            reference) or SEMB_DM_SIGNED (dm projected on the
+                            azimuth direction, so A sees its sign) */
 } semb_params;
 
 /* Fill `p` with the defaults for `method` (grid fields zero, batched FP16 with

@@ -92,6 +92,7 @@ int main(int argc, const char** argv) {
   g_flags["-mode"] = "Search form: plain (default) or batched";
   g_flags["-store"] = "Trace storage of the batched form: f16 (default), bf16 or f32";
   g_flags["-d"] = "CUDA device";
+  if (method == SEMB_CRS) g_flags["-dm"] = "Midpoint displacement: abs (default, as the reference) or signed (along -azimuth)";
   parse(argc, argv);
 
   semb_params p;
@@ -131,6 +132,12 @@ int main(int argc, const char** argv) {
   else if (store == "bf16") p.storage = SEMB_STORE_BF16;
   else if (store == "f32") p.storage = SEMB_STORE_F32;
   else die_help();
+  if (method == SEMB_CRS) {
+    const std::string dm = get("-dm", false, "abs");
+    if (dm == "abs") p.dm_mode = SEMB_DM_ABS;
+    else if (dm == "signed") p.dm_mode = SEMB_DM_SIGNED;
+    else die_help();
+  }
 
   semb_survey* survey = nullptr;
   check(semb_survey_load(path.c_str(), method, p.aph, &survey), "reading input");

@@ -198,6 +198,8 @@ int check_params(const semb_params* p) {
   if (ncand > (1 << 24)) return fail(SEMB_E_ARG, "candidate grid of %lld is too large", (long long)ncand);
   if (p->storage < SEMB_STORE_F32 || p->storage > SEMB_STORE_BF16) return fail(SEMB_E_ARG, "unknown storage");
   if (p->repick < 0 || p->repick > 2) return fail(SEMB_E_ARG, "unknown repick mode");
+  if (p->dm_mode != SEMB_DM_ABS && p->dm_mode != SEMB_DM_SIGNED) return fail(SEMB_E_ARG, "unknown dm_mode");
+  if (!std::isfinite(p->azimuth)) return fail(SEMB_E_ARG, "azimuth must be finite");
   if (!(p->tau >= 0.0) || !std::isfinite(p->tau)) return fail(SEMB_E_ARG, "tau must be a non-negative number");
   return SEMB_OK;
 }
@@ -614,9 +616,14 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   SEMB_TRY(dev_alloc(&pl->d_ap_tr, pl->nap));
   SEMB_TRY(dev_alloc(&pl->d_ap_geo, pl->nap));
   SEMB_TRY(dev_alloc(&pl->d_ap_geo64, pl->nap));
+  // azimuth direction for the signed midpoint displacement (SEMB_DM_SIGNED)
+  const double az = p.azimuth * 3.14159265358979323846 / 180.0;
+  const double cos_d = std::cos(az), sin_d = std::sin(az);
   k_aperture_fill<<<(g->ncdps + 7) / 8, 256, 0, st>>>(g->ncdps, p.method, pl->d_nbr_off, pl->d_nbr, d_cdp_end,
                                                        pl->d_ap_off, d_h32, d_mx32, d_my32, d_h64, d_mx64, d_my64,
-                                                       pl->d_ap_tr, pl->d_ap_geo, pl->d_ap_geo64);
+                                                       pl->d_ap_tr, pl->d_ap_geo, pl->d_ap_geo64,
+                                                       p.dm_mode == SEMB_DM_SIGNED ? 1 : 0, (float)cos_d,
+                                                       (float)sin_d, cos_d, sin_d);
   SEMB_CUDA(cudaGetLastError());
   int max_ap = 0;
   for (int i = 0; i < g->ncdps; ++i) max_ap = std::max<int64_t>(max_ap, ap_off[i + 1] - ap_off[i]);

@@ -158,14 +158,17 @@ static __global__ void k_aperture_count(int ncdps, const int64_t* __restrict__ n
 // Aperture entries of CDP i (one warp per CDP): the traces of its neighbours in
 // list order, each trace's |dm|, dm^2 and h relative to the midpoint of CDP i's
 // first trace (CRS/OpenMP/src/main.cpp:179-204, 289-317), in float and in double.
-// CMP apertures are the CDP's own traces with dm = 0.
+// With `signed_dm` (SEMB_DM_SIGNED, no reference counterpart) dm is the midpoint
+// displacement projected on the azimuth direction (cos, sin), signed, and dm^2 its
+// square.  CMP apertures are the CDP's own traces with dm = 0.
 static __global__ void k_aperture_fill(int ncdps, int method, const int64_t* __restrict__ nbr_off,
                                 const int32_t* __restrict__ nbr, const int64_t* __restrict__ cdp_end,
                                 const int64_t* __restrict__ ap_off, const float* __restrict__ h32,
                                 const float* __restrict__ mx32, const float* __restrict__ my32,
                                 const double* __restrict__ h64, const double* __restrict__ mx64,
                                 const double* __restrict__ my64, int32_t* __restrict__ ap_tr,
-                                float4* __restrict__ ap_geo, Geo64* __restrict__ ap_geo64) {
+                                float4* __restrict__ ap_geo, Geo64* __restrict__ ap_geo64, int signed_dm,
+                                float cos_f, float sin_f, double cos_d, double sin_d) {
   const int warps = blockDim.x >> 5;
   const int i = blockIdx.x * warps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -180,7 +183,14 @@ static __global__ void k_aperture_fill(int ncdps, int method, const int64_t* __r
     for (int64_t t = t0 + lane; t < t1; t += 32) {
       const int64_t e = pos + (t - t0);
       ap_tr[e] = (int32_t)t;
-      if (method == METHOD_CRS) {
+      if (method == METHOD_CRS && signed_dm) {
+        const float dx = __fsub_rn(mx32[t], cx), dy = __fsub_rn(my32[t], cy);
+        const float m = __fadd_rn(__fmul_rn(dx, cos_f), __fmul_rn(dy, sin_f));
+        ap_geo[e] = make_float4(m, __fmul_rn(m, m), h32[t], 0.f);
+        const double dxd = __dsub_rn(mx64[t], cxd), dyd = __dsub_rn(my64[t], cyd);
+        const double md = __dadd_rn(__dmul_rn(dxd, cos_d), __dmul_rn(dyd, sin_d));
+        ap_geo64[e] = Geo64{md, __dmul_rn(md, md), h64[t], 0.0};
+      } else if (method == METHOD_CRS) {
         const float dx = __fsub_rn(mx32[t], cx), dy = __fsub_rn(my32[t], cy);
         const float m2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
         ap_geo[e] = make_float4(__fsqrt_rn(m2), m2, h32[t], 0.f);

@@ -254,8 +254,10 @@ __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_
     t2min = T_lo * T_lo + fminf(pb[4] * g.z, pb[5] * g.z);
     t2max = T_hi * T_hi + fmaxf(pb[4] * g.z, pb[5] * g.z);
   } else {
-    // t^2 = (t0 + a*m)^2 + b*m2 + c*h with m, m2, h >= 0
-    float ulo = T_lo + pb[0] * g.x, uhi = T_hi + pb[1] * g.x;
+    // t^2 = (t0 + a*m)^2 + b*m2 + c*h with m2, h >= 0; m >= 0, or signed along the
+    // azimuth
+    const float am0 = pb[0] * g.x, am1 = pb[1] * g.x;
+    float ulo = T_lo + fminf(am0, am1), uhi = T_hi + fmaxf(am0, am1);
     float u2lo = (ulo <= 0.f && uhi >= 0.f) ? 0.f : fminf(ulo * ulo, uhi * uhi);
     float u2hi = fmaxf(ulo * ulo, uhi * uhi);
     t2min = u2lo + pb[2] * g.y + pb[4] * g.z;

@@ -28,7 +28,8 @@ CMP, CRS = 0, 1
 PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
-ABI_VERSION = 3
+DM_ABS, DM_SIGNED = 0, 1
+ABI_VERSION = 4
 MAX_VARIANTS = 16   # SEMB_MAX_VARIANTS
 MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
@@ -50,7 +51,7 @@ class SembParams(C.Structure):
         ("na", C.c_int32), ("nb", C.c_int32), ("nc", C.c_int32),
         ("aph", C.c_int32), ("apm", C.c_int32), ("storage", C.c_int32),
         ("tau", C.c_double), ("azimuth", C.c_double),
-        ("repick", C.c_int32), ("repick_gap", C.c_float),
+        ("repick", C.c_int32), ("repick_gap", C.c_float), ("dm_mode", C.c_int32),
     ]
 
 
@@ -144,13 +145,13 @@ def _ptr(a: np.ndarray | None):
 
 
 def params(method: int, mode: int = PLAIN_F32, storage: int = STORE_F16, repick: int = REPICK_NEAR_TIES,
-           repick_gap: float = 3e-4, **kw) -> SembParams:
+           repick_gap: float = 3e-4, dm_mode: int = DM_ABS, **kw) -> SembParams:
     """Build semb_params from the reference's flag names (c0, c1, nc, aph, tau, and
     for CRS a0, a1, na, b0, b1, nb, apm, azimuth).  CMP values are rounded to float
     first, as the reference's stof does."""
     p = SembParams()
     lib().semb_params_init(C.byref(p), method)
-    p.mode, p.storage, p.repick, p.repick_gap = mode, storage, repick, repick_gap
+    p.mode, p.storage, p.repick, p.repick_gap, p.dm_mode = mode, storage, repick, repick_gap, dm_mode
     rnd = (lambda v: float(np.float32(v))) if method == CMP else float
     for k in ("a0", "a1", "b0", "b1", "c0", "c1", "tau", "azimuth"):
         if k in kw:

@@ -55,6 +55,7 @@ def lib():
                           P, P, P, P, P, P, P, P, P, P, i32]
         _lib.semb_oracle_max_threads.restype = i32
         _lib.semb_oracle_set_threads.argtypes = [i32]
+        _lib.semb_oracle_set_dm.argtypes = [i32, f64]
     return _lib
 
 
@@ -168,12 +169,15 @@ def cmp(g: dict, params: dict, precision: str = "f32", sem_all: bool = False, th
 
 
 def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, threads: int = 0,
-        cdps=None) -> dict:
+        cdps=None, dm_signed: bool = False) -> dict:
     """CRS search of the gather (all CDPs, or only the CDP indices in `cdps`, with
-    the neighbour lists of the whole gather)."""
+    the neighbour lists of the whole gather).  `dm_signed` switches the midpoint
+    displacement to the signed projection on params["azimuth"] (the library's
+    SEMB_DM_SIGNED, which has no reference counterpart)."""
     L = lib()
     if threads:
         L.semb_oracle_set_threads(threads)
+    L.semb_oracle_set_dm(1 if dm_signed else 0, float(params.get("azimuth", 0.0)))
     real = np.float32 if precision == "f32" else np.float64
     ncdp, ns = len(g["cdp_ids"]), g["ns"]
     na, nb, nc = int(params["na"]), int(params["nb"]), int(params["nc"])

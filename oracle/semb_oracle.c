@@ -25,6 +25,10 @@
 #define MAX_W_CMP 16
 #define MAX_W_CRS 5
 
+/* CRS midpoint displacement switch, read by the restatement (semb_oracle_set_dm) */
+static int semb_oracle_dm_signed = 0;
+static double semb_oracle_dm_cos = 1.0, semb_oracle_dm_sin = 0.0;
+
 #define REAL float
 #define SQRTR sqrtf
 #define SFX _f32
@@ -43,3 +47,14 @@
 
 int semb_oracle_max_threads(void) { return omp_get_max_threads(); }
 void semb_oracle_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }
+
+/* CRS midpoint displacement of the next searches: 0 = |dm| (the reference), 1 =
+ * dm projected on the azimuth direction (cos, sin), signed, with dm^2 = dm * dm.
+ * The signed operator is this build's extension (SEMB_DM_SIGNED); the reference
+ * has no counterpart, so this branch restates the library's definition. */
+void semb_oracle_set_dm(int signed_dm, double azimuth_deg) {
+  const double az = azimuth_deg * 3.14159265358979323846 / 180.0;
+  semb_oracle_dm_signed = signed_dm ? 1 : 0;
+  semb_oracle_dm_cos = cos(az);
+  semb_oracle_dm_sin = sin(az);
+}

@@ -248,9 +248,16 @@ int CAT(semb_oracle_crs, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
       for (int it = 0; it < t_idf - t_id0; it++) {
         REAL dx = m0x[t_id0 + it] - m0x_cdp_id;
         REAL dy = m0y[t_id0 + it] - m0y_cdp_id;
-        REAL _m2 = dx * dx + dy * dy;
-        m2[size + it] = _m2;
-        m[size + it] = SQRTR(_m2);
+        if (semb_oracle_dm_signed) {
+          /* signed displacement along the azimuth (no reference counterpart) */
+          const REAL md = dx * (REAL)semb_oracle_dm_cos + dy * (REAL)semb_oracle_dm_sin;
+          m[size + it] = md;
+          m2[size + it] = md * md;
+        } else {
+          REAL _m2 = dx * dx + dy * dy;
+          m2[size + it] = _m2;
+          m[size + it] = SQRTR(_m2);
+        }
         h[size + it] = h0[t_id0 + it];
       }
       size += t_idf - t_id0;

@@ -84,3 +84,30 @@ def test_bounded_wait_gives_up_and_device_stays_usable():
     (ctr, sem, stk), _ = _run(semb.CMP, g, s.params, mode=semb.PLAIN_F32)
     ref = oracle.cmp(g, s.params, "f32")
     assert np.array_equal(ctr, ref["ctr"])
+
+
+@pytest.mark.parametrize("azimuth", [30.0, 90.0])
+def test_crs_signed_dm_plain_matches_oracle_f32(azimuth):
+    """SEMB_DM_SIGNED (dm projected on the azimuth, signed): the plain form against
+    the oracle's signed branch in single precision."""
+    s = synth.crs_survey(seed=42, ncdp=12, noffsets=16, ns=300, na=5, nb=3, nc=4, tau=0.004, azimuth=azimuth)
+    p = dict(s.params)
+    g = oracle.gather(s.headers, s.samples, "crs", p["aph"], p["apm"], real=np.float32)
+    ref = oracle.crs(g, p, "f32", dm_signed=True)
+    (ctr, sem, stk), _ = _run(semb.CRS, g, p, mode=semb.PLAIN_F32, dm_mode=semb.DM_SIGNED)
+    assert np.array_equal(ctr, ref["ctr"])
+    np.testing.assert_allclose(sem, ref["str"], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(stk, ref["stk"], rtol=1e-5, atol=1e-6)
+
+
+def test_crs_signed_dm_batched_close_to_oracle_f64():
+    s = synth.crs_survey(seed=43, ncdp=12, noffsets=16, ns=300, na=5, nb=5, nc=5, azimuth=30.0)
+    p = dict(s.params)
+    g = oracle.gather(s.headers, s.samples, "crs", p["aph"], p["apm"], real=np.float64)
+    ref = oracle.crs(g, p, "f64", dm_signed=True)
+    (ctr, sem, stk), _ = _run(semb.CRS, g, p, mode=semb.BATCHED, dm_mode=semb.DM_SIGNED)
+    assert np.max(np.abs(sem - ref["str"])) < 1e-3
+    assert np.mean(ctr == ref["ctr"]) > 0.99
+    # and it is not the |dm| result
+    absr = oracle.crs(g, p, "f64")
+    assert not np.allclose(absr["str"], ref["str"])
