@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 4
+#define SEMB_ABI_VERSION 5
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
 #define SEMB_MAX_VARIANTS 16
@@ -95,6 +95,9 @@ typedef struct semb_params {
   int32_t dm_mode;       /* CRS midpoint displacement: SEMB_DM_ABS (|dm|, as the
                             reference) or SEMB_DM_SIGNED (dm projected on the
                             azimuth direction, so A sees its sign) */
+  int32_t attrs;         /* batched form: 1 keeps the extra attribute outputs of
+                            semb_plan_download_attrs (second-best candidate, FP64
+                            error of the pick); 0 (default) does not */
 } semb_params;
 
 /* Fill `p` with the defaults for `method` (grid fields zero, batched FP16 with
@@ -150,6 +153,13 @@ int semb_survey_view(const semb_survey* s, semb_gather_view* out);
 int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t* ctr,
                       const float* str, const float* stk, const char* out_dir);
 
+/* Write one extra attribute file out_dir/name: one trace per CDP in the survey's
+ * CDP order with the CDP's first trace header unchanged (as the coherence file) and
+ * the ns samples data[i * ns ...].  For the attribute grids of
+ * semb_plan_download_attrs (e.g. "crs.coher2.su", "crs.err64.su"); an aperture map
+ * is a per-CDP count spread over ns samples.  No counterpart in the reference. */
+int semb_survey_write_attr(const semb_survey* s, const char* name, const float* data, const char* out_dir);
+
 void semb_survey_free(semb_survey* s);
 
 /* ---- search (device) -------------------------------------------------------- */
@@ -184,6 +194,19 @@ int semb_plan_run(semb_plan* plan);
  * semblance; CRS: linear index ia*nb*nc + ib*nc + ic), str = semblance, stk = stack.
  * These are the reference's ctr/str/stk arrays (CRS/OpenMP/src/main.cpp:126-128). */
 int semb_plan_download(semb_plan* plan, int32_t* ctr, float* str, float* stk);
+
+/* Extra attributes of the last run (any pointer may be NULL):
+ *   sem2, idx2 [ncdps * ns]  second-best candidate: the best candidate other than the
+ *                            pick, by single-precision semblance (0 and -1 where
+ *                            there is none); batched form with attrs = 1
+ *   err64 [ncdps * ns]       |single-precision semblance - FP64 semblance| of the
+ *                            pick where the FP64 re-pick evaluated it, -1 elsewhere
+ *                            (every (CDP, t0) with repick = SEMB_REPICK_ALWAYS);
+ *                            batched form with attrs = 1
+ *   aperture [ncdps]         aperture traces of each CDP (its fold for CMP); any form
+ * SEMB_E_STATE when an attribute of the batched form is asked of a plan without it.
+ * No counterpart in the reference. */
+int semb_plan_download_attrs(semb_plan* plan, float* sem2, int32_t* idx2, float* err64, int32_t* aperture);
 
 /* Copy the device-built neighbour lists (CRS): off[ncdps+1], list[off[ncdps]]
  * (pass list = NULL to query the size in *n_out).  The lists are those of

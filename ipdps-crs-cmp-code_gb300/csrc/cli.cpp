@@ -93,6 +93,7 @@ int main(int argc, const char** argv) {
   g_flags["-store"] = "Trace storage of the batched form: f16 (default), bf16 or f32";
   g_flags["-d"] = "CUDA device";
   if (method == SEMB_CRS) g_flags["-dm"] = "Midpoint displacement: abs (default, as the reference) or signed (along -azimuth)";
+  g_flags["-attrs"] = "1: also write <method>.aperture.su and, batched, <method>.coher2.su and <method>.err64.su";
   parse(argc, argv);
 
   semb_params p;
@@ -139,6 +140,9 @@ int main(int argc, const char** argv) {
     else die_help();
   }
 
+  const bool attrs = std::atoi(get("-attrs", false, "0").c_str()) != 0;
+  p.attrs = attrs && p.mode == SEMB_BATCHED ? 1 : 0;
+
   semb_survey* survey = nullptr;
   check(semb_survey_load(path.c_str(), method, p.aph, &survey), "reading input");
   semb_gather_view v;
@@ -169,6 +173,25 @@ int main(int argc, const char** argv) {
                 (double)s.evals / (s.ms_total * 1e-3));
   info(__FILE__, __LINE__, line);
   check(semb_survey_write(survey, &p, ctr.data(), str.data(), stk.data(), "."), "writing outputs");
+  if (attrs) {
+    // extra attribute files: aperture map (any form); second-best semblance and the
+    // FP64 error of the pick (batched form)
+    const std::string pre = method == SEMB_CMP ? "cmp." : "crs.";
+    std::vector<int32_t> ap(v.ncdps);
+    std::vector<float> buf(n);
+    if (p.mode == SEMB_BATCHED) {
+      std::vector<float> sem2(n), err(n);
+      std::vector<int32_t> idx2(n);
+      check(semb_plan_download_attrs(plan, sem2.data(), idx2.data(), err.data(), ap.data()), "downloading attributes");
+      check(semb_survey_write_attr(survey, (pre + "coher2.su").c_str(), sem2.data(), "."), "writing outputs");
+      check(semb_survey_write_attr(survey, (pre + "err64.su").c_str(), err.data(), "."), "writing outputs");
+    } else {
+      check(semb_plan_download_attrs(plan, nullptr, nullptr, nullptr, ap.data()), "downloading attributes");
+    }
+    for (int i = 0; i < v.ncdps; ++i)
+      for (int q = 0; q < v.ns; ++q) buf[(size_t)i * v.ns + q] = (float)ap[i];
+    check(semb_survey_write_attr(survey, (pre + "aperture.su").c_str(), buf.data(), "."), "writing outputs");
+  }
   semb_plan_destroy(plan);
   semb_survey_free(survey);
   return EXIT_SUCCESS;

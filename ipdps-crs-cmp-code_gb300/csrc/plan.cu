@@ -112,6 +112,11 @@ struct semb_plan {
   float* d_top_stk = nullptr;
   int* d_status = nullptr;
   unsigned long long* d_repicked = nullptr;
+  // extra attributes (batched form with attrs = 1)
+  float* d_sem2 = nullptr;
+  int32_t* d_idx2 = nullptr;
+  float* d_err64 = nullptr;
+  std::vector<int32_t> aperture;   // aperture traces per CDP (host copy)
 
   cudaEvent_t ev[6] = {};
   bool use_graph = false;
@@ -183,6 +188,9 @@ void free_data(semb_plan* pl) {
   dev_free(pl->d_top_sem);
   dev_free(pl->d_top_idx);
   dev_free(pl->d_top_stk);
+  dev_free(pl->d_sem2);
+  dev_free(pl->d_idx2);
+  dev_free(pl->d_err64);
   if (pl->graph) cudaGraphExecDestroy(pl->graph);
   pl->graph = nullptr;
   pl->uploaded = false;
@@ -199,6 +207,7 @@ int check_params(const semb_params* p) {
   if (p->storage < SEMB_STORE_F32 || p->storage > SEMB_STORE_BF16) return fail(SEMB_E_ARG, "unknown storage");
   if (p->repick < 0 || p->repick > 2) return fail(SEMB_E_ARG, "unknown repick mode");
   if (p->dm_mode != SEMB_DM_ABS && p->dm_mode != SEMB_DM_SIGNED) return fail(SEMB_E_ARG, "unknown dm_mode");
+  if (p->attrs != 0 && p->attrs != 1) return fail(SEMB_E_ARG, "attrs must be 0 or 1");
   if (!std::isfinite(p->azimuth)) return fail(SEMB_E_ARG, "azimuth must be finite");
   if (!(p->tau >= 0.0) || !std::isfinite(p->tau)) return fail(SEMB_E_ARG, "tau must be a non-negative number");
   return SEMB_OK;
@@ -725,7 +734,14 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
     SEMB_TRY(dev_alloc(&pl->d_top_sem, nout * kTopK));
     SEMB_TRY(dev_alloc(&pl->d_top_idx, nout * kTopK));
     SEMB_TRY(dev_alloc(&pl->d_top_stk, nout * kTopK));
+    if (p.attrs) {
+      SEMB_TRY(dev_alloc(&pl->d_sem2, nout));
+      SEMB_TRY(dev_alloc(&pl->d_idx2, nout));
+      SEMB_TRY(dev_alloc(&pl->d_err64, nout));
+    }
   }
+  pl->aperture.resize(g->ncdps);
+  for (int i = 0; i < g->ncdps; ++i) pl->aperture[i] = (int32_t)(ap_off[i + 1] - ap_off[i]);
 
   // the default variant of this method and window; variant 0 where it does not fit
   if (set_all(pl, default_variant(p.method, form, pl->w)) != SEMB_OK) SEMB_TRY(set_all(pl, 0));
@@ -853,6 +869,9 @@ int enqueue_run(semb_plan* pl, bool timed) {
     R.str = pl->d_str;
     R.stk = pl->d_stk;
     R.repicked = pl->d_repicked;
+    R.sem2 = pl->d_sem2;
+    R.idx2 = pl->d_idx2;
+    R.err64 = pl->d_err64;
     SEMB_CUDA(cudaMemsetAsync(pl->d_repicked, 0, sizeof(unsigned long long), st));
     SEMB_TRY(launch_repick(pl->w, R, st));
     ++launches;
@@ -932,6 +951,22 @@ int semb_plan_download(semb_plan* pl, int32_t* ctr, float* str, float* stk) {
   if (str) SEMB_CUDA(cudaMemcpyAsync(str, pl->d_str, n * 4, cudaMemcpyDeviceToHost, st));
   if (stk) SEMB_CUDA(cudaMemcpyAsync(stk, pl->d_stk, n * 4, cudaMemcpyDeviceToHost, st));
   SEMB_CUDA(cudaStreamSynchronize(st));
+  return SEMB_OK;
+}
+
+int semb_plan_download_attrs(semb_plan* pl, float* sem2, int32_t* idx2, float* err64, int32_t* aperture) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_download_attrs before semb_plan_upload");
+  if ((sem2 || idx2 || err64) && !pl->d_sem2)
+    return fail(SEMB_E_STATE, "second-best and FP64-error attributes need the batched form with attrs = 1");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  const size_t n = (size_t)pl->ncdps * pl->ns;
+  cudaStream_t st = pl->stream;
+  if (sem2) SEMB_CUDA(cudaMemcpyAsync(sem2, pl->d_sem2, n * 4, cudaMemcpyDeviceToHost, st));
+  if (idx2) SEMB_CUDA(cudaMemcpyAsync(idx2, pl->d_idx2, n * 4, cudaMemcpyDeviceToHost, st));
+  if (err64) SEMB_CUDA(cudaMemcpyAsync(err64, pl->d_err64, n * 4, cudaMemcpyDeviceToHost, st));
+  SEMB_CUDA(cudaStreamSynchronize(st));
+  if (aperture) std::memcpy(aperture, pl->aperture.data(), pl->aperture.size() * sizeof(int32_t));
   return SEMB_OK;
 }
 

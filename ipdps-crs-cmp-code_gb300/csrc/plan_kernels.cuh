@@ -302,6 +302,10 @@ struct RepickParams {
   float* str;
   float* stk;
   unsigned long long* repicked;
+  // extra attributes (null when the plan does not keep them)
+  float* sem2;     // second-best candidate's single-precision semblance
+  int32_t* idx2;   // and its grid index (-1: none)
+  float* err64;    // |FP32 - FP64 semblance| of the pick where re-evaluated, else -1
 };
 
 // Final pick per (CDP, t0), one warp each.  When the best two FP32 candidates are
@@ -323,6 +327,9 @@ static __global__ void k_repick(RepickParams R) {
     ti[q] = R.top_idx[item * kTopK + q];
     tk[q] = R.top_stk[item * kTopK + q];
   }
+  int ti0[kTopK];   // the list before the candidates out of reach are dropped
+#pragma unroll
+  for (int q = 0; q < kTopK; ++q) ti0[q] = ti[q];
   const bool none = !(ts[0] > 0.f) || ti[0] < 0;
   const bool near_tie = ti[1] >= 0 && ts[1] > 0.f && (ts[0] - ts[1]) < R.gap;
   const bool redo = !none && (R.mode == 2 || (R.mode == 1 && near_tie));
@@ -333,6 +340,7 @@ static __global__ void k_repick(RepickParams R) {
     if (ti[q] >= 0 && !(R.mode == 2 || (ts[0] - ts[q]) < R.gap)) ti[q] = -1;
   int out_i = ti[0];
   float out_s = ts[0], out_k = tk[0];
+  float err = -1.f;
   if (redo) {
     double num[kTopK][W], den[kTopK], lin[kTopK];
     int M[kTopK];
@@ -421,8 +429,27 @@ static __global__ void k_repick(RepickParams R) {
       out_i = bi;
       out_s = (float)bs;
       out_k = (float)bk;
+#pragma unroll
+      for (int q = 0; q < kTopK; ++q)
+        if (ti0[q] == bi) err = (float)fabs((double)ts[q] - bs);
     }
     if (lane == 0) atomicAdd(R.repicked, 1ull);
+  }
+  if (R.sem2 && lane == 0) {
+    // the best single-precision candidate other than the pick
+    float s2 = 0.f;
+    int i2 = -1;
+    if (!none) {
+#pragma unroll
+      for (int q = kTopK - 1; q >= 0; --q)
+        if (ti0[q] >= 0 && ts[q] > 0.f && ti0[q] != out_i) {
+          s2 = ts[q];
+          i2 = ti0[q];
+        }
+    }
+    R.sem2[item] = s2;
+    R.idx2[item] = i2;
+    R.err64[item] = err;
   }
   if (lane == 0) {
     if (none) {

@@ -343,6 +343,21 @@ int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t*
   return ok ? SEMB_OK : fail(SEMB_E_IO, "write error");
 }
 
+int semb_survey_write_attr(const semb_survey* s, const char* name, const float* data, const char* out_dir) {
+  if (!s || !name || !*name || !data) return fail(SEMB_E_ARG, "null argument");
+  const std::string dir = (out_dir && *out_dir) ? std::string(out_dir) + "/" : std::string();
+  const std::string path = dir + name;
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return fail(SEMB_E_IO, "cannot create %s: %s", path.c_str(), std::strerror(errno));
+  const int ncdps = (int)s->cdp_end.size(), ns = s->ns;
+  bool ok = true;
+  for (int i = 0; i < ncdps && ok; ++i)
+    ok = std::fwrite(&s->first_hdr[(size_t)i * kHdrSize], 1, kHdrSize, f) == (size_t)kHdrSize &&
+         std::fwrite(data + (size_t)i * ns, sizeof(float), (size_t)ns, f) == (size_t)ns;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? SEMB_OK : fail(SEMB_E_IO, "write error");
+}
+
 void semb_survey_free(semb_survey* s) { delete s; }
 
 const char* semb_strerror(int code) {

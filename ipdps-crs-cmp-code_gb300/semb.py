@@ -29,7 +29,7 @@ PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
 DM_ABS, DM_SIGNED = 0, 1
-ABI_VERSION = 4
+ABI_VERSION = 5
 MAX_VARIANTS = 16   # SEMB_MAX_VARIANTS
 MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
@@ -38,6 +38,7 @@ OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODE
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
+    "semb_plan_download_attrs", "semb_survey_write_attr",
     "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
     "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
@@ -52,6 +53,7 @@ class SembParams(C.Structure):
         ("aph", C.c_int32), ("apm", C.c_int32), ("storage", C.c_int32),
         ("tau", C.c_double), ("azimuth", C.c_double),
         ("repick", C.c_int32), ("repick_gap", C.c_float), ("dm_mode", C.c_int32),
+        ("attrs", C.c_int32),
     ]
 
 
@@ -102,11 +104,13 @@ def lib():
         "semb_survey_from_bytes": (C.c_int, [P, i64, i32, i32, P]),
         "semb_survey_view": (C.c_int, [P, P]),
         "semb_survey_write": (C.c_int, [P, P, P, P, P, C.c_char_p]),
+        "semb_survey_write_attr": (C.c_int, [P, C.c_char_p, P, C.c_char_p]),
         "semb_survey_free": (None, [P]),
         "semb_plan_create": (C.c_int, [P, i32, P]),
         "semb_plan_upload": (C.c_int, [P, P]),
         "semb_plan_run": (C.c_int, [P]),
         "semb_plan_download": (C.c_int, [P, P, P, P]),
+        "semb_plan_download_attrs": (C.c_int, [P, P, P, P, P]),
         "semb_plan_neighbours": (C.c_int, [P, P, P, P]),
         "semb_plan_stats": (C.c_int, [P, P]),
         "semb_neighbours_noalloc": (C.c_int, [P, P, P, P, P, i32, i32, P, P, i64, P, P]),
@@ -145,13 +149,13 @@ def _ptr(a: np.ndarray | None):
 
 
 def params(method: int, mode: int = PLAIN_F32, storage: int = STORE_F16, repick: int = REPICK_NEAR_TIES,
-           repick_gap: float = 3e-4, dm_mode: int = DM_ABS, **kw) -> SembParams:
+           repick_gap: float = 3e-4, dm_mode: int = DM_ABS, attrs: int = 0, **kw) -> SembParams:
     """Build semb_params from the reference's flag names (c0, c1, nc, aph, tau, and
     for CRS a0, a1, na, b0, b1, nb, apm, azimuth).  CMP values are rounded to float
     first, as the reference's stof does."""
     p = SembParams()
     lib().semb_params_init(C.byref(p), method)
-    p.mode, p.storage, p.repick, p.repick_gap, p.dm_mode = mode, storage, repick, repick_gap, dm_mode
+    p.mode, p.storage, p.repick, p.repick_gap, p.dm_mode, p.attrs = mode, storage, repick, repick_gap, dm_mode, attrs
     rnd = (lambda v: float(np.float32(v))) if method == CMP else float
     for k in ("a0", "a1", "b0", "b1", "c0", "c1", "tau", "azimuth"):
         if k in kw:
@@ -241,6 +245,12 @@ class Survey:
         _check(lib().semb_survey_write(self._h, C.byref(p), _ptr(ctr), _ptr(sem), _ptr(stk),
                                        str(out_dir).encode()), "semb_survey_write")
 
+    def write_attr(self, name: str, data, out_dir: str) -> None:
+        """One extra attribute file: a trace of ns samples per CDP (first-trace header)."""
+        data = np.ascontiguousarray(data, np.float32)
+        _check(lib().semb_survey_write_attr(self._h, name.encode(), _ptr(data), str(out_dir).encode()),
+               "semb_survey_write_attr")
+
     def close(self) -> None:
         if self._h:
             lib().semb_survey_free(self._h)
@@ -280,6 +290,21 @@ class Plan:
         stk = np.empty(n, np.float32) if stk is None else stk
         _check(lib().semb_plan_download(self._h, _ptr(ctr), _ptr(sem), _ptr(stk)), "semb_plan_download")
         return (ctr.reshape(self.ncdps, self.ns), sem.reshape(self.ncdps, self.ns), stk.reshape(self.ncdps, self.ns))
+
+    def download_attrs(self, batched: bool = True) -> dict:
+        """Extra attributes of the last run: aperture traces per CDP and, for a batched
+        plan made with attrs=1, the second-best candidate (sem2, idx2) and the FP64
+        error of the pick (err64, -1 where not re-evaluated)."""
+        n = self.ncdps * self.ns
+        ap = np.empty(self.ncdps, np.int32)
+        if not batched:
+            _check(lib().semb_plan_download_attrs(self._h, None, None, None, _ptr(ap)), "semb_plan_download_attrs")
+            return {"aperture": ap}
+        sem2, idx2, err = np.empty(n, np.float32), np.empty(n, np.int32), np.empty(n, np.float32)
+        _check(lib().semb_plan_download_attrs(self._h, _ptr(sem2), _ptr(idx2), _ptr(err), _ptr(ap)),
+               "semb_plan_download_attrs")
+        shp = (self.ncdps, self.ns)
+        return {"aperture": ap, "sem2": sem2.reshape(shp), "idx2": idx2.reshape(shp), "err64": err.reshape(shp)}
 
     def neighbours(self):
         n = C.c_int64()

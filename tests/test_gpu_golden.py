@@ -100,6 +100,27 @@ def test_cli_end_to_end(case, tmp_path):
     np.testing.assert_allclose(mine["stack"][1][same], ref["stack"][1][same], rtol=2e-5, atol=tol)
 
 
+@pytest.mark.parametrize("case", ["cmp_line", "crs_line"])
+def test_cli_attribute_files(case, tmp_path):
+    """-attrs 1 -mode batched also writes the aperture map, the second-best semblance
+    and the FP64 error of the pick, one trace per CDP like the coherence file."""
+    meta, h, s, path = G.load(case)
+    method = meta["method"]
+    exe = os.path.join(BUILD, f"{method}-gb300")
+    r = subprocess.run([exe] + meta["args"] + ["-i", path, "-mode", "batched", "-attrs", "1"], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    import su
+    hc, coher = su.read_su(str(tmp_path / f"{method}.coher.su"))
+    for name in ("aperture", "coher2", "err64"):
+        hx, x = su.read_su(str(tmp_path / f"{method}.{name}.su"))
+        assert hx.tobytes() == hc.tobytes() and x.shape == coher.shape, name
+    _, ap = su.read_su(str(tmp_path / f"{method}.aperture.su"))
+    assert np.all(ap >= 1) and np.all(ap == ap[:, :1])
+    _, c2 = su.read_su(str(tmp_path / f"{method}.coher2.su"))
+    assert np.all(c2 <= coher + 1e-3)
+
+
 def test_graph_replay_matches_direct_launch():
     meta, h, s, path = G.load("crs_uneven_w5")
     p = meta["params"]

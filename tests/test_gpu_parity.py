@@ -111,3 +111,35 @@ def test_crs_signed_dm_batched_close_to_oracle_f64():
     # and it is not the |dm| result
     absr = oracle.crs(g, p, "f64")
     assert not np.allclose(absr["str"], ref["str"])
+
+
+def test_attribute_outputs():
+    """Extra attributes: the aperture map, the second-best candidate and the FP64
+    error of the pick (every (CDP, t0) re-evaluated with repick = ALWAYS)."""
+    s = synth.crs_survey(seed=44, ncdp=12, noffsets=16, ns=300, na=5, nb=5, nc=5)
+    p = dict(s.params)
+    g = oracle.gather(s.headers, s.samples, "crs", p["aph"], p["apm"], real=np.float64)
+    ref = oracle.crs(g, p, "f64")
+    folds = np.diff(np.concatenate([[0], g["ntraces_by_cdp_id"]]))
+    ap_ref = np.array([folds[g["nbr"][g["nbr_off"][i]:g["nbr_off"][i + 1]]].sum() for i in range(len(folds))])
+    with semb.Plan(semb.params(semb.CRS, mode=semb.BATCHED, repick=semb.REPICK_ALWAYS, attrs=1, **p)) as plan:
+        plan.upload(_arrays(g).view())
+        plan.run()
+        ctr, sem, stk = plan.download()
+        at = plan.download_attrs()
+    assert np.array_equal(at["aperture"], ap_ref)
+    picked = sem > 0
+    # the FP64 error of every pick is known, small, and the pick's value is the FP64 one
+    assert np.all(at["err64"][picked] >= 0) and np.max(at["err64"][picked]) < 1e-3
+    np.testing.assert_allclose(sem[picked], ref["str"][picked], rtol=1e-6, atol=1e-7)
+    # second best: another candidate, not better than the pick beyond FP32 error
+    has2 = at["idx2"] >= 0
+    assert np.mean(has2[picked]) > 0.9
+    assert np.all(at["idx2"][has2] != ctr[has2])
+    assert np.all(at["sem2"][has2] <= sem[has2] + 1e-3)
+    # a plain plan has the aperture map only
+    with semb.Plan(semb.params(semb.CRS, mode=semb.PLAIN_F32, **p)) as plain:
+        plain.upload(_arrays(g).view())
+        assert np.array_equal(plain.download_attrs(batched=False)["aperture"], ap_ref)
+        with pytest.raises(semb.SembError):
+            plain.download_attrs()

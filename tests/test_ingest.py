@@ -114,3 +114,24 @@ def test_offset_aperture_filter(semb_lib):
     for aph in (0, int(np.median(hx)), int(hx.max())):
         a = semb.Survey.load(path, semb.CMP, aph).arrays()
         assert a["ntraces"] == int(np.sum(hx <= aph))
+
+
+@pytest.mark.parametrize("case", ["cmp_line", "crs_line"])
+def test_attribute_writer(case, semb_lib):
+    """semb_survey_write_attr: one trace per CDP in the survey's order, the CDP's first
+    trace header unchanged (as the coherence file), the given samples."""
+    meta, h, s, path = G.load(case)
+    method, p = meta["method"], meta["params"]
+    sv = semb.Survey.load(path, METHOD[method], p["aph"])
+    a = sv.arrays()
+    ncdp, ns = len(a["cdp"]), a["ns"]
+    data = np.arange(ncdp * ns, dtype=np.float32).reshape(ncdp, ns) * np.float32(0.5)
+    ctr = np.zeros((ncdp, ns), np.int32)
+    sem = np.zeros((ncdp, ns), np.float32)
+    with tempfile.TemporaryDirectory() as d:
+        sv.write(semb.params(METHOD[method], **p), ctr, sem, sem, d)
+        sv.write_attr(f"{method}.extra.su", data, d)
+        hx, sx = su.read_su(os.path.join(d, f"{method}.extra.su"))
+        hc, _ = su.read_su(os.path.join(d, f"{method}.coher.su"))
+    assert np.array_equal(sx, data)
+    assert hx.tobytes() == hc.tobytes()
