@@ -38,6 +38,10 @@ constexpr int kBucketAp[kBucketSplits] = {1024, 384, 128};
 static_assert(kBucketSplits + 1 <= kMaxBuckets, "bucket table");
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int default_variant(int method, int form, int w);
+int grid_neighbours(int ncdps, const float* d_fmx, const float* d_fmy, int apm, int64_t* d_off, int32_t** d_list,
+                    int64_t* n_out, cudaStream_t st);
+// CDP count from which the CRS neighbour lists come from the grid search
+constexpr int kGridNeighbours = 2048;
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);
 
@@ -594,13 +598,18 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   SEMB_TRY(dev_alloc(&pl->d_nbr_off, g->ncdps + 1));
   if (p.method == SEMB_CRS) {
     k_cdp_midpoints<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_cdp_end, d_gx, d_gy, d_sx, d_sy, d_sc, d_fmx, d_fmy);
-    const float lim = (float)((int32_t)p.apm * (int32_t)p.apm);
-    k_neighbours<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_fmx, d_fmy, lim, d_cnt32, nullptr, nullptr);
-    k_scan_exclusive<int32_t><<<1, 1024, 0, st>>>(g->ncdps, d_cnt32, pl->d_nbr_off);
-    SEMB_CUDA(cudaMemcpyAsync(&pl->n_nbr, pl->d_nbr_off + g->ncdps, 8, cudaMemcpyDeviceToHost, st));
-    SEMB_CUDA(cudaStreamSynchronize(st));
-    SEMB_TRY(dev_alloc(&pl->d_nbr, (size_t)pl->n_nbr));
-    k_neighbours<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_fmx, d_fmy, lim, nullptr, pl->d_nbr_off, pl->d_nbr);
+    if (g->ncdps >= kGridNeighbours) {
+      // large surveys: grid cells + sorts, O(n log n); the same lists
+      SEMB_TRY(grid_neighbours(g->ncdps, d_fmx, d_fmy, p.apm, pl->d_nbr_off, &pl->d_nbr, &pl->n_nbr, st));
+    } else {
+      const float lim = (float)((int32_t)p.apm * (int32_t)p.apm);
+      k_neighbours<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_fmx, d_fmy, lim, d_cnt32, nullptr, nullptr);
+      k_scan_exclusive<int32_t><<<1, 1024, 0, st>>>(g->ncdps, d_cnt32, pl->d_nbr_off);
+      SEMB_CUDA(cudaMemcpyAsync(&pl->n_nbr, pl->d_nbr_off + g->ncdps, 8, cudaMemcpyDeviceToHost, st));
+      SEMB_CUDA(cudaStreamSynchronize(st));
+      SEMB_TRY(dev_alloc(&pl->d_nbr, (size_t)pl->n_nbr));
+      k_neighbours<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_fmx, d_fmy, lim, nullptr, pl->d_nbr_off, pl->d_nbr);
+    }
   } else {
     std::vector<int64_t> off(g->ncdps + 1);
     std::vector<int32_t> lst(g->ncdps);

@@ -143,3 +143,31 @@ def test_attribute_outputs():
         assert np.array_equal(plain.download_attrs(batched=False)["aperture"], ap_ref)
         with pytest.raises(semb.SembError):
             plain.download_attrs()
+
+
+def test_grid_neighbour_lists_match_the_reference_rule():
+    """Surveys of 2048 CDPs or more get their CRS neighbour lists from the grid
+    search (cells + sorts); they equal the reference's all-pairs lists.  A 3D layout
+    (a 55 x 55 grid of CDPs, 10 m apart, apm 25 m) has neighbours along x and y."""
+    import su
+    n1, ns = 55, 32
+    ix, iy = np.meshgrid(np.arange(n1), np.arange(n1), indexing="ij")
+    h = su.empty_headers(n1 * n1)
+    h["cdp"] = np.arange(1, n1 * n1 + 1)
+    h["scalco"] = -100
+    # midpoints on the grid (cm), half-offset 50 m along x, with a little jitter
+    rng = np.random.default_rng(46)
+    mx = (ix.ravel() * 1000 + rng.integers(-40, 40, n1 * n1)).astype(np.int32)
+    my = (iy.ravel() * 1000 + rng.integers(-40, 40, n1 * n1)).astype(np.int32)
+    h["sx"], h["gx"], h["sy"], h["gy"] = mx - 5000, mx + 5000, my, my
+    h["ns"], h["dt"] = ns, 4000
+    samples = rng.standard_normal((n1 * n1, ns)).astype(np.float32)
+    p = dict(a0=-1e-3, a1=1e-3, na=1, b0=0.0, b1=0.0, nb=1, c0=2e-7, c1=1e-6, nc=1, aph=100, apm=25, tau=0.0)
+    g = oracle.gather(h, samples, "crs", p["aph"], p["apm"], real=np.float32)
+    assert len(g["cdp_ids"]) >= 2048
+    with semb.Plan(semb.params(semb.CRS, mode=semb.PLAIN_F32, **p)) as plan:
+        plan.upload(_arrays(g).view())
+        off, lst = plan.neighbours()
+    assert np.array_equal(off, g["nbr_off"])
+    assert np.array_equal(lst, g["nbr"])
+    assert np.max(np.diff(off)) >= 9   # neighbours along x and y
