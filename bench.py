@@ -54,7 +54,11 @@ WORKLOADS = {
     "crs-500x48": (2, None, semb.CRS),
     "crs-uneven-2000": (3, 2000, semb.CRS),
     "crs-uneven-20k": (3, None, semb.CRS),
+    # the 100k-CDP, 31^3-grid survey with BF16 traces; --ncdp runs its first N CDPs
+    "crs-100k-31cubed": (4, 1000, semb.CRS),
 }
+# trace storage of the workloads whose survey names one (else --storage, f16)
+WORKLOAD_STORAGE = {"crs-100k-31cubed": "bf16"}
 
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -393,7 +397,8 @@ def run_ours(args, rank, world, dist):
                        "ns": st["ns"], "ncand": st["ncand"], "window": st["window"], "traces": s.ntraces,
                        "mean_aperture": nap / st["ncdps"], "trace_evals_per_step": st["trace_evals"],
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (FP16 store %.2f GB)" % (s.samples.nbytes / 2e9),
+                       "l2": "inputs larger than L2 (%s store %.2f GB)" % (
+                           args.storage.upper(), s.samples.nbytes / (1e9 if args.storage == "f32" else 2e9)),
                        "graph": bool(args.graph)},
             "plain_f32": res["plain"], "batched": res["batched"],
             "speedup_batched_vs_plain": res["plain"]["ms"] / (total_ms / args.steps),
@@ -426,7 +431,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="cmp-4096-uneven")
     ap.add_argument("--ncdp", type=int, default=None)
-    ap.add_argument("--storage", choices=["f16", "bf16", "f32"], default="f16")
+    ap.add_argument("--storage", choices=["f16", "bf16", "f32"], default=None)
     ap.add_argument("--graph", type=int, default=1)
     ap.add_argument("--tune", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=0)
@@ -434,6 +439,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true")
     args = ap.parse_args()
+    if args.storage is None:
+        args.storage = WORKLOAD_STORAGE.get(args.workload, "f16")
     if args.warmup < 3:
         log("warm-up raised to 3 steps (timing rule)")
         args.warmup = 3
