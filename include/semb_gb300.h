@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 5
+#define SEMB_ABI_VERSION 6
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
 #define SEMB_MAX_VARIANTS 16
@@ -98,6 +98,10 @@ typedef struct semb_params {
   int32_t attrs;         /* batched form: 1 keeps the extra attribute outputs of
                             semb_plan_download_attrs (second-best candidate, FP64
                             error of the pick); 0 (default) does not */
+  int32_t ngen;          /* CRS, plain form: > 0 runs CRS-DE (-ngen of the reference's
+                            crs-ocl-de) instead of the grid search: differential
+                            evolution of na*nb*nc individuals (<= 256) for ngen
+                            generations; 0 (default) is the grid search */
 } semb_params;
 
 /* Fill `p` with the defaults for `method` (grid fields zero, batched FP16 with
@@ -160,6 +164,11 @@ int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t*
  * is a per-CDP count spread over ns samples.  No counterpart in the reference. */
 int semb_survey_write_attr(const semb_survey* s, const char* name, const float* data, const char* out_dir);
 
+/* The CRS output files from explicit parameter values (CRS-DE): crs.{a,b,c,coher,
+ * stack}.su as semb_survey_write writes them, with a/b/c [ncdps * ns] taken as given. */
+int semb_survey_write_abc(const semb_survey* s, const float* a, const float* b, const float* c, const float* str,
+                          const float* stk, const char* out_dir);
+
 void semb_survey_free(semb_survey* s);
 
 /* ---- search (device) -------------------------------------------------------- */
@@ -207,6 +216,12 @@ int semb_plan_download(semb_plan* plan, int32_t* ctr, float* str, float* stk);
  * SEMB_E_STATE when an attribute of the batched form is asked of a plan without it.
  * No counterpart in the reference. */
 int semb_plan_download_attrs(semb_plan* plan, float* sem2, int32_t* idx2, float* err64, int32_t* aperture);
+
+/* CRS-DE results of the last run: the picked A, B, C per (CDP, t0) (C in s^2/m^2);
+ * semblance and stack come from semb_plan_download, whose ctr is -1 for CRS-DE (the
+ * pick is not a grid index).  SEMB_E_STATE for a grid-search plan.  Replaces the
+ * result arrays of crs-ocl-de (README.md:86-106). */
+int semb_plan_download_abc(semb_plan* plan, float* a, float* b, float* c);
 
 /* Copy the device-built neighbour lists (CRS): off[ncdps+1], list[off[ncdps]]
  * (pass list = NULL to query the size in *n_out).  The lists are those of

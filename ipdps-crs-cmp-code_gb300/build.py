@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp
                      "-I" + INCLUDE, "-I" + CSRC]
 
 LIB_SOURCES = ["su_io.cpp", "plan.cu", "launch.cu", "search_cmp_plain.cu", "search_cmp_fast.cu",
-               "search_crs_plain.cu", "search_crs_fast.cu", "probe.cu", "noalloc.cu", "neighbours.cu"]
+               "search_crs_plain.cu", "search_crs_fast.cu", "probe.cu", "noalloc.cu", "neighbours.cu", "de.cu"]
 
 
 def nvcc() -> str:

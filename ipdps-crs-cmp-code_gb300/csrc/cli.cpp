@@ -93,6 +93,7 @@ int main(int argc, const char** argv) {
   g_flags["-store"] = "Trace storage of the batched form: f16 (default), bf16 or f32";
   g_flags["-d"] = "CUDA device";
   if (method == SEMB_CRS) g_flags["-dm"] = "Midpoint displacement: abs (default, as the reference) or signed (along -azimuth)";
+  if (method == SEMB_CRS) g_flags["-ngen"] = "Generations of the CRS-DE search (differential evolution; 0: grid search)";
   g_flags["-attrs"] = "1: also write <method>.aperture.su and, batched, <method>.coher2.su and <method>.err64.su";
   parse(argc, argv);
 
@@ -134,6 +135,11 @@ int main(int argc, const char** argv) {
   else if (store == "f32") p.storage = SEMB_STORE_F32;
   else die_help();
   if (method == SEMB_CRS) {
+    try {
+      p.ngen = std::stoi(get("-ngen", false, "0"));
+    } catch (const std::exception& e) {
+      FAIL(std::string("bad numeric argument: ") + e.what());
+    }
     const std::string dm = get("-dm", false, "abs");
     if (dm == "abs") p.dm_mode = SEMB_DM_ABS;
     else if (dm == "signed") p.dm_mode = SEMB_DM_SIGNED;
@@ -172,7 +178,14 @@ int main(int argc, const char** argv) {
   std::snprintf(line, sizeof(line), "Kernel Time: %f, Semblance evaluations/s: %.6e", s.ms_total * 1e-3,
                 (double)s.evals / (s.ms_total * 1e-3));
   info(__FILE__, __LINE__, line);
-  check(semb_survey_write(survey, &p, ctr.data(), str.data(), stk.data(), "."), "writing outputs");
+  if (p.ngen > 0) {
+    std::vector<float> av(n), bv(n), cv(n);
+    check(semb_plan_download_abc(plan, av.data(), bv.data(), cv.data()), "downloading results");
+    check(semb_survey_write_abc(survey, av.data(), bv.data(), cv.data(), str.data(), stk.data(), "."),
+          "writing outputs");
+  } else {
+    check(semb_survey_write(survey, &p, ctr.data(), str.data(), stk.data(), "."), "writing outputs");
+  }
   if (attrs) {
     // extra attribute files: aperture map (any form); second-best semblance and the
     // FP64 error of the pick (batched form)

@@ -44,6 +44,7 @@ int grid_neighbours(int ncdps, const float* d_fmx, const float* d_fmy, int apm, 
 constexpr int kGridNeighbours = 2048;
 int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);
+int launch_crs_de(int w, const DeParams& R, cudaStream_t st);
 
 }  // namespace semb
 
@@ -121,6 +122,11 @@ struct semb_plan {
   int32_t* d_idx2 = nullptr;
   float* d_err64 = nullptr;
   std::vector<int32_t> aperture;   // aperture traces per CDP (host copy)
+  // CRS-DE (ngen > 0): the single-precision grid and the picked parameters
+  float* d_grid = nullptr;
+  float* d_de_a = nullptr;
+  float* d_de_b = nullptr;
+  float* d_de_c = nullptr;
 
   cudaEvent_t ev[6] = {};
   bool use_graph = false;
@@ -195,6 +201,10 @@ void free_data(semb_plan* pl) {
   dev_free(pl->d_sem2);
   dev_free(pl->d_idx2);
   dev_free(pl->d_err64);
+  dev_free(pl->d_grid);
+  dev_free(pl->d_de_a);
+  dev_free(pl->d_de_b);
+  dev_free(pl->d_de_c);
   if (pl->graph) cudaGraphExecDestroy(pl->graph);
   pl->graph = nullptr;
   pl->uploaded = false;
@@ -212,6 +222,11 @@ int check_params(const semb_params* p) {
   if (p->repick < 0 || p->repick > 2) return fail(SEMB_E_ARG, "unknown repick mode");
   if (p->dm_mode != SEMB_DM_ABS && p->dm_mode != SEMB_DM_SIGNED) return fail(SEMB_E_ARG, "unknown dm_mode");
   if (p->attrs != 0 && p->attrs != 1) return fail(SEMB_E_ARG, "attrs must be 0 or 1");
+  if (p->ngen < 0) return fail(SEMB_E_ARG, "ngen must be >= 0");
+  if (p->ngen > 0 && (p->method != SEMB_CRS || p->mode != SEMB_PLAIN_F32))
+    return fail(SEMB_E_ARG, "CRS-DE (ngen > 0) is a CRS search of the plain form");
+  if (p->ngen > 0 && ncand > 256) return fail(SEMB_E_ARG, "CRS-DE population na*nb*nc = %lld above 256",
+                                              (long long)ncand);
   if (!std::isfinite(p->azimuth)) return fail(SEMB_E_ARG, "azimuth must be finite");
   if (!(p->tau >= 0.0) || !std::isfinite(p->tau)) return fail(SEMB_E_ARG, "tau must be a non-negative number");
   return SEMB_OK;
@@ -749,6 +764,20 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
       SEMB_TRY(dev_alloc(&pl->d_err64, nout));
     }
   }
+  if (p.ngen > 0) {
+    std::vector<float> grid(3 * (size_t)pl->ncand);
+    for (int i = 0; i < pl->ncand; ++i) {
+      grid[3 * (size_t)i] = pl->ga[i];
+      grid[3 * (size_t)i + 1] = pl->gb[i];
+      grid[3 * (size_t)i + 2] = pl->gc[i];
+    }
+    SEMB_TRY(dev_alloc(&pl->d_grid, grid.size()));
+    SEMB_CUDA(cudaMemcpyAsync(pl->d_grid, grid.data(), grid.size() * 4, cudaMemcpyHostToDevice, st));
+    SEMB_CUDA(cudaStreamSynchronize(st));
+    SEMB_TRY(dev_alloc(&pl->d_de_a, nout));
+    SEMB_TRY(dev_alloc(&pl->d_de_b, nout));
+    SEMB_TRY(dev_alloc(&pl->d_de_c, nout));
+  }
   pl->aperture.resize(g->ncdps);
   for (int i = 0; i < g->ncdps; ++i) pl->aperture[i] = (int32_t)(ap_off[i + 1] - ap_off[i]);
 
@@ -843,6 +872,45 @@ int enqueue_run(semb_plan* pl, bool timed) {
   if (p.method == SEMB_CRS) {
     SEMB_TRY(launch_stt00(pl->w, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
     ++launches;
+  }
+  if (p.ngen > 0) {
+    // CRS-DE: differential evolution per (CDP, t0) instead of the grid search
+    DeParams D{};
+    D.samples = pl->d_samples;
+    D.pitch = pl->pitch;
+    D.ap_off = pl->d_ap_off;
+    D.ap_tr = pl->d_ap_tr;
+    D.ap_geo = pl->d_ap_geo;
+    D.grid = pl->d_grid;
+    D.lo[0] = (float)p.a0;
+    D.lo[1] = (float)p.b0;
+    D.lo[2] = (float)(p.c0 * kFactor);
+    D.hi[0] = (float)p.a1;
+    D.hi[1] = (float)p.b1;
+    D.hi[2] = (float)(p.c1 * kFactor);
+    D.np = pl->ncand;
+    D.ngen = p.ngen;
+    D.ncdps = pl->ncdps;
+    D.ns = pl->ns;
+    D.tau = pl->tau;
+    D.dt = pl->dt;
+    D.idt = pl->idt;
+    D.stt00 = pl->d_stt00;
+    D.a = pl->d_de_a;
+    D.b = pl->d_de_b;
+    D.c = pl->d_de_c;
+    D.str = pl->d_str;
+    D.stk = pl->d_stk;
+    SEMB_CUDA(cudaMemsetAsync(pl->d_ctr, 0xff, (size_t)pl->ncdps * pl->ns * 4, st));
+    if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[1], st));
+    SEMB_TRY(launch_crs_de(pl->w, D, st));
+    ++launches;
+    if (timed) {
+      SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
+      SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
+    }
+    pl->stats.kernel_launches = launches;
+    return SEMB_OK;
   }
   if (form == FORM_FAST) SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, kMaxBuckets * sizeof(int), st));
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[1], st));
@@ -976,6 +1044,20 @@ int semb_plan_download_attrs(semb_plan* pl, float* sem2, int32_t* idx2, float* e
   if (err64) SEMB_CUDA(cudaMemcpyAsync(err64, pl->d_err64, n * 4, cudaMemcpyDeviceToHost, st));
   SEMB_CUDA(cudaStreamSynchronize(st));
   if (aperture) std::memcpy(aperture, pl->aperture.data(), pl->aperture.size() * sizeof(int32_t));
+  return SEMB_OK;
+}
+
+int semb_plan_download_abc(semb_plan* pl, float* a, float* b, float* c) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_download_abc before semb_plan_upload");
+  if (!pl->d_de_a) return fail(SEMB_E_STATE, "explicit A, B, C are the results of CRS-DE (ngen > 0)");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  const size_t n = (size_t)pl->ncdps * pl->ns;
+  cudaStream_t st = pl->stream;
+  if (a) SEMB_CUDA(cudaMemcpyAsync(a, pl->d_de_a, n * 4, cudaMemcpyDeviceToHost, st));
+  if (b) SEMB_CUDA(cudaMemcpyAsync(b, pl->d_de_b, n * 4, cudaMemcpyDeviceToHost, st));
+  if (c) SEMB_CUDA(cudaMemcpyAsync(c, pl->d_de_c, n * 4, cudaMemcpyDeviceToHost, st));
+  SEMB_CUDA(cudaStreamSynchronize(st));
   return SEMB_OK;
 }
 

@@ -284,6 +284,25 @@ static __global__ void k_crs_stt00(int ncdps, KParams P, float a, float b, float
   out[cdp] = ok ? __fdiv_rn(lin, __fmul_rn((float)W, mf)) : 0.0f;
 }
 
+// CRS-DE launch parameters (csrc/de.cu)
+struct DeParams {
+  const float* samples;   // FP32 store [ntr][pitch]
+  int64_t pitch;
+  const int64_t* ap_off;
+  const int32_t* ap_tr;
+  const float4* ap_geo;   // (|dm| or signed dm, dm^2, h) in float
+  const float* grid;      // [np][3]: the single-precision search grid (C 1e6-scaled)
+  float lo[3], hi[3];     // search box
+  int np, ngen, ncdps, ns, tau;
+  float dt, idt;
+  const float* stt00;     // stack of item (t0 = 0, candidate 0) per CDP
+  float* a;               // picked parameters per (CDP, t0); C back in s^2/m^2
+  float* b;
+  float* c;
+  float* str;
+  float* stk;
+};
+
 struct RepickParams {
   const float* top_sem;
   const int32_t* top_idx;

@@ -343,6 +343,45 @@ int semb_survey_write(const semb_survey* s, const semb_params* p, const int32_t*
   return ok ? SEMB_OK : fail(SEMB_E_IO, "write error");
 }
 
+int semb_survey_write_abc(const semb_survey* s, const float* a, const float* b, const float* c, const float* str,
+                          const float* stk, const char* out_dir) {
+  if (!s || !a || !b || !c || !str || !stk) return fail(SEMB_E_ARG, "null argument");
+  if (s->method != SEMB_CRS) return fail(SEMB_E_ARG, "explicit A, B, C outputs are CRS files");
+  const std::string dir = (out_dir && *out_dir) ? std::string(out_dir) + "/" : std::string();
+  const char* names[] = {"crs.a.su", "crs.b.su", "crs.c.su", "crs.coher.su", "crs.stack.su"};
+  const float* data[] = {a, b, c, str, stk};
+  FILE* f[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  for (int k = 0; k < 5; ++k) {
+    const std::string path = dir + names[k];
+    f[k] = std::fopen(path.c_str(), "wb");
+    if (!f[k]) {
+      for (int q = 0; q < k; ++q) std::fclose(f[q]);
+      return fail(SEMB_E_IO, "cannot create %s: %s", path.c_str(), std::strerror(errno));
+    }
+  }
+  const int ncdps = (int)s->cdp_end.size(), ns = s->ns;
+  unsigned char hdr0[kHdrSize], hdr[kHdrSize];
+  bool ok = true;
+  for (int i = 0; i < ncdps && ok; ++i) {
+    // headers as semb_survey_write: parameter files with offset 0 and the integer
+    // midpoint, coherence and stack files with the first trace's header
+    std::memcpy(hdr0, &s->first_hdr[(size_t)i * kHdrSize], kHdrSize);
+    std::memcpy(hdr, hdr0, kHdrSize);
+    const int32_t mx = (int32_t)(((int64_t)rd_i32(hdr, kOffSx) + rd_i32(hdr, kOffGx)) >> 1);
+    const int32_t my = (int32_t)(((int64_t)rd_i32(hdr, kOffSy) + rd_i32(hdr, kOffGy)) >> 1);
+    wr_i32(hdr, kOffOffset, 0);
+    wr_i32(hdr, kOffSx, mx);
+    wr_i32(hdr, kOffGx, mx);
+    wr_i32(hdr, kOffSy, my);
+    wr_i32(hdr, kOffGy, my);
+    for (int k = 0; k < 5 && ok; ++k)
+      ok = std::fwrite(k < 3 ? hdr : hdr0, 1, kHdrSize, f[k]) == (size_t)kHdrSize &&
+           std::fwrite(data[k] + (size_t)i * ns, sizeof(float), (size_t)ns, f[k]) == (size_t)ns;
+  }
+  for (int k = 0; k < 5; ++k) ok = (std::fclose(f[k]) == 0) && ok;
+  return ok ? SEMB_OK : fail(SEMB_E_IO, "write error");
+}
+
 int semb_survey_write_attr(const semb_survey* s, const char* name, const float* data, const char* out_dir) {
   if (!s || !name || !*name || !data) return fail(SEMB_E_ARG, "null argument");
   const std::string dir = (out_dir && *out_dir) ? std::string(out_dir) + "/" : std::string();

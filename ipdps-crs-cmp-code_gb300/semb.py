@@ -29,7 +29,7 @@ PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
 DM_ABS, DM_SIGNED = 0, 1
-ABI_VERSION = 5
+ABI_VERSION = 6
 MAX_VARIANTS = 16   # SEMB_MAX_VARIANTS
 MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
@@ -38,7 +38,7 @@ OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODE
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
-    "semb_plan_download_attrs", "semb_survey_write_attr",
+    "semb_plan_download_attrs", "semb_survey_write_attr", "semb_plan_download_abc", "semb_survey_write_abc",
     "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
     "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
@@ -53,7 +53,7 @@ class SembParams(C.Structure):
         ("aph", C.c_int32), ("apm", C.c_int32), ("storage", C.c_int32),
         ("tau", C.c_double), ("azimuth", C.c_double),
         ("repick", C.c_int32), ("repick_gap", C.c_float), ("dm_mode", C.c_int32),
-        ("attrs", C.c_int32),
+        ("attrs", C.c_int32), ("ngen", C.c_int32),
     ]
 
 
@@ -111,6 +111,8 @@ def lib():
         "semb_plan_run": (C.c_int, [P]),
         "semb_plan_download": (C.c_int, [P, P, P, P]),
         "semb_plan_download_attrs": (C.c_int, [P, P, P, P, P]),
+        "semb_plan_download_abc": (C.c_int, [P, P, P, P]),
+        "semb_survey_write_abc": (C.c_int, [P, P, P, P, P, P, C.c_char_p]),
         "semb_plan_neighbours": (C.c_int, [P, P, P, P]),
         "semb_plan_stats": (C.c_int, [P, P]),
         "semb_neighbours_noalloc": (C.c_int, [P, P, P, P, P, i32, i32, P, P, i64, P, P]),
@@ -149,13 +151,15 @@ def _ptr(a: np.ndarray | None):
 
 
 def params(method: int, mode: int = PLAIN_F32, storage: int = STORE_F16, repick: int = REPICK_NEAR_TIES,
-           repick_gap: float = 3e-4, dm_mode: int = DM_ABS, attrs: int = 0, **kw) -> SembParams:
+           repick_gap: float = 3e-4, dm_mode: int = DM_ABS, attrs: int = 0, ngen: int = 0,
+           **kw) -> SembParams:
     """Build semb_params from the reference's flag names (c0, c1, nc, aph, tau, and
     for CRS a0, a1, na, b0, b1, nb, apm, azimuth).  CMP values are rounded to float
     first, as the reference's stof does."""
     p = SembParams()
     lib().semb_params_init(C.byref(p), method)
     p.mode, p.storage, p.repick, p.repick_gap, p.dm_mode, p.attrs = mode, storage, repick, repick_gap, dm_mode, attrs
+    p.ngen = ngen
     rnd = (lambda v: float(np.float32(v))) if method == CMP else float
     for k in ("a0", "a1", "b0", "b1", "c0", "c1", "tau", "azimuth"):
         if k in kw:
@@ -245,6 +249,12 @@ class Survey:
         _check(lib().semb_survey_write(self._h, C.byref(p), _ptr(ctr), _ptr(sem), _ptr(stk),
                                        str(out_dir).encode()), "semb_survey_write")
 
+    def write_abc(self, a, b, c, sem, stk, out_dir: str) -> None:
+        """crs.{a,b,c,coher,stack}.su from explicit parameter values (CRS-DE)."""
+        arr = [np.ascontiguousarray(x, np.float32) for x in (a, b, c, sem, stk)]
+        _check(lib().semb_survey_write_abc(self._h, *[_ptr(x) for x in arr], str(out_dir).encode()),
+               "semb_survey_write_abc")
+
     def write_attr(self, name: str, data, out_dir: str) -> None:
         """One extra attribute file: a trace of ns samples per CDP (first-trace header)."""
         data = np.ascontiguousarray(data, np.float32)
@@ -290,6 +300,14 @@ class Plan:
         stk = np.empty(n, np.float32) if stk is None else stk
         _check(lib().semb_plan_download(self._h, _ptr(ctr), _ptr(sem), _ptr(stk)), "semb_plan_download")
         return (ctr.reshape(self.ncdps, self.ns), sem.reshape(self.ncdps, self.ns), stk.reshape(self.ncdps, self.ns))
+
+    def download_abc(self):
+        """CRS-DE: the picked A, B, C per (CDP, t0) (C in s^2/m^2)."""
+        n = self.ncdps * self.ns
+        a, b, c = (np.empty(n, np.float32) for _ in range(3))
+        _check(lib().semb_plan_download_abc(self._h, _ptr(a), _ptr(b), _ptr(c)), "semb_plan_download_abc")
+        shp = (self.ncdps, self.ns)
+        return a.reshape(shp), b.reshape(shp), c.reshape(shp)
 
     def download_attrs(self, batched: bool = True) -> dict:
         """Extra attributes of the last run: aperture traces per CDP and, for a batched

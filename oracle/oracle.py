@@ -56,6 +56,12 @@ def lib():
         _lib.semb_oracle_max_threads.restype = i32
         _lib.semb_oracle_set_threads.argtypes = [i32]
         _lib.semb_oracle_set_dm.argtypes = [i32, f64]
+        for sfx in ("_f32", "_f64"):
+            f = getattr(_lib, "semb_oracle_crs_de" + sfx)
+            f.restype = i32
+            f.argtypes = [i32, P, i32, i32, P, P, P, P, P, P, P, P,
+                          f64, f64, i32, f64, f64, i32, f64, f64, i32, f64, i32,
+                          P, P, P, P, P, P, i32]
     return _lib
 
 
@@ -205,6 +211,33 @@ def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, th
     if sem_all:
         out["sem_all"] = sem.reshape(ncdp, ns, npar)
     return out
+
+
+def crs_de(g: dict, params: dict, ngen: int, precision: str = "f32", threads: int = 0, cdps=None,
+           dm_signed: bool = False) -> dict:
+    """CRS-DE search (differential evolution over A, B, C; the library's definition,
+    restated in semb_oracle_body.h) of the gather: picked a, b, c, semblance, stack."""
+    L = lib()
+    if threads:
+        L.semb_oracle_set_threads(threads)
+    L.semb_oracle_set_dm(1 if dm_signed else 0, float(params.get("azimuth", 0.0)))
+    real = np.float32 if precision == "f32" else np.float64
+    ncdp, ns = len(g["cdp_ids"]), g["ns"]
+    strr = np.zeros(ncdp * ns, real)
+    stk = np.zeros(ncdp * ns, real)
+    oa, ob, oc = (np.zeros(ncdp * ns, np.float32) for _ in range(3))
+    P = lambda k: parsed("crs", params[k])
+    lst, nlst = _list(cdps)
+    fn = getattr(L, "semb_oracle_crs_de_" + precision)
+    rc = fn(ncdp, _p(g["ntraces_by_cdp_id"]), ns, g["dt_us"], _p(g["samples"]),
+            _p(g["gx"]), _p(g["gy"]), _p(g["sx"]), _p(g["sy"]), _p(g["scalco"]),
+            _p(g["nbr_off"]), _p(g["nbr"]),
+            P("a0"), P("a1"), int(params["na"]), P("b0"), P("b1"), int(params["nb"]), P("c0"), P("c1"),
+            int(params["nc"]), P("tau"), int(ngen), _p(oa), _p(ob), _p(oc), _p(strr), _p(stk), _p(lst), nlst)
+    if rc != 0:
+        raise RuntimeError(f"oracle crs_de failed: {rc}")
+    shp = (ncdp, ns)
+    return dict(a=oa.reshape(shp), b=ob.reshape(shp), c=oc.reshape(shp), str=strr.reshape(shp), stk=stk.reshape(shp))
 
 
 REF_OUTPUTS = {"cmp": ["c", "coher", "stack"], "crs": ["a", "b", "c", "coher", "stack"]}
