@@ -27,7 +27,20 @@ def _case(seed=61, **kw):
     return s, p, oracle.gather(s.headers, s.samples, "crs", p["aph"], p["apm"], real=np.float32)
 
 
-@pytest.mark.parametrize("ngen", [0, 1, 15])
+def test_zero_generations_is_the_grid_search():
+    """ngen = 0 is the plan's grid search, whose picks the DE restatement reproduces
+    from its starting population."""
+    s, p, g = _case()
+    ref = oracle.crs_de(g, p, 0, "f32")
+    with semb.Plan(semb.params(semb.CRS, mode=semb.PLAIN_F32, **p)) as plan:
+        plan.upload(_arrays(g).view())
+        plan.run()
+        ctr, sem, stk = plan.download()
+    assert np.all(ctr >= 0)
+    assert np.array_equal(sem, ref["str"]) and np.array_equal(stk, ref["stk"])
+
+
+@pytest.mark.parametrize("ngen", [1, 15])
 def test_de_matches_oracle_f32(ngen):
     s, p, g = _case()
     ref = oracle.crs_de(g, p, ngen, "f32")
