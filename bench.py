@@ -332,15 +332,27 @@ def run_ours(args, rank, world, dist):
             plan.download(ctr.array, sem.array, stk.array)
         barrier()
         t0 = time.perf_counter()
+        phase = [0.0, 0.0, 0.0]   # upload, run, download (host wall time)
+        up_dev = 0.0              # upload's device time (CUDA events)
         for _ in range(args.steps):
+            ta = time.perf_counter()
             plan.upload(arrays.view())
+            tb = time.perf_counter()
             plan.run()
+            tc = time.perf_counter()
             plan.download(ctr.array, sem.array, stk.array)
+            td = time.perf_counter()
+            phase[0] += tb - ta
+            phase[1] += tc - tb
+            phase[2] += td - tc
+            up_dev += plan.stats()["ms_upload"]
         e2e_s = max_over_ranks(time.perf_counter() - t0)
         h2d = s.samples.nbytes + 5 * 4 * s.ntraces + 8 * len(cdp_end)
         d2h = 3 * 4 * st["ncdps"] * st["ns"]
         e2e = {"value": world * evals * args.steps / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s / args.steps * 1e3}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s / args.steps * 1e3,
+               "ms_upload": phase[0] / args.steps * 1e3, "ms_upload_device": up_dev / args.steps,
+               "ms_run": phase[1] / args.steps * 1e3, "ms_download": phase[2] / args.steps * 1e3}
         ctr.free(), sem.free(), stk.free()
 
     # error of the batched form against the FP64 oracle on a sample

@@ -15,6 +15,7 @@
 #include <cstdint>
 #include <cstring>
 #include <numeric>
+#include <unordered_map>
 #include <vector>
 
 #include "common.h"
@@ -128,6 +129,9 @@ struct semb_plan {
   float* d_de_b = nullptr;
   float* d_de_c = nullptr;
 
+  // bytes held by each buffer that a later upload of the same size reuses
+  std::unordered_map<const void*, size_t> caps;
+
   cudaEvent_t ev[6] = {};
   bool use_graph = false;
   cudaGraphExec_t graph = nullptr;
@@ -177,34 +181,55 @@ void drop_graph(semb_plan* pl) {
   pl->graph = nullptr;
 }
 
-void free_data(semb_plan* pl) {
-  dev_free(pl->d_samples);
-  dev_free(pl->d_samples16);
-  dev_free(pl->d_scale);
-  dev_free(pl->d_ap_off);
-  dev_free(pl->d_ap_tr);
-  dev_free(pl->d_ap_geo);
-  dev_free(pl->d_ap_geo64);
-  dev_free(pl->d_nbr_off);
-  dev_free(pl->d_nbr);
+// Device buffer *p of n elements, kept from the previous upload when it is large
+// enough (re-uploads of a survey of the same size then allocate nothing).
+template <typename T>
+int dev_reuse(semb_plan* pl, T** p, size_t n) {
+  const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  auto it = pl->caps.find(p);
+  if (*p && it != pl->caps.end() && it->second >= bytes) return SEMB_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  pl->caps.erase(p);
+  SEMB_TRY(dev_alloc(p, n));
+  pl->caps[p] = bytes;
+  return SEMB_OK;
+}
+
+// Free the plan's data; with keep_reusable the buffers dev_reuse manages stay.
+void free_data(semb_plan* pl, bool keep_reusable = false) {
+  auto release = [&](auto& ptr) {
+    if (keep_reusable && pl->caps.count(&ptr)) return;
+    pl->caps.erase(&ptr);
+    dev_free(ptr);
+  };
+  release(pl->d_samples);
+  release(pl->d_samples16);
+  release(pl->d_scale);
+  release(pl->d_ap_off);
+  release(pl->d_ap_tr);
+  release(pl->d_ap_geo);
+  release(pl->d_ap_geo64);
+  release(pl->d_nbr_off);
+  release(pl->d_nbr);
   for (Bucket& b : pl->buckets) free_cfg(b.cfg);
   pl->buckets.clear();
-  dev_free(pl->d_cand64);
-  dev_free(pl->d_tasks);
-  dev_free(pl->d_ctr);
-  dev_free(pl->d_str);
-  dev_free(pl->d_stk);
-  dev_free(pl->d_stt00);
-  dev_free(pl->d_top_sem);
-  dev_free(pl->d_top_idx);
-  dev_free(pl->d_top_stk);
-  dev_free(pl->d_sem2);
-  dev_free(pl->d_idx2);
-  dev_free(pl->d_err64);
-  dev_free(pl->d_grid);
-  dev_free(pl->d_de_a);
-  dev_free(pl->d_de_b);
-  dev_free(pl->d_de_c);
+  release(pl->d_cand64);
+  release(pl->d_tasks);
+  release(pl->d_ctr);
+  release(pl->d_str);
+  release(pl->d_stk);
+  release(pl->d_stt00);
+  release(pl->d_top_sem);
+  release(pl->d_top_idx);
+  release(pl->d_top_stk);
+  release(pl->d_sem2);
+  release(pl->d_idx2);
+  release(pl->d_err64);
+  release(pl->d_grid);
+  release(pl->d_de_a);
+  release(pl->d_de_b);
+  release(pl->d_de_c);
   if (pl->graph) cudaGraphExecDestroy(pl->graph);
   pl->graph = nullptr;
   pl->uploaded = false;
@@ -537,7 +562,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   if (prev != g->ntraces) return fail(SEMB_E_ARG, "cdp_end[ncdps-1] must equal ntraces");
 
   SEMB_CUDA(cudaSetDevice(pl->device));
-  free_data(pl);
+  free_data(pl, true);
   cudaStream_t st = pl->stream;
   pl->ncdps = g->ncdps;
   pl->ns = g->ns;
@@ -567,7 +592,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   cudaEventRecord(pl->ev[4], st);
   // trace store
   const int64_t ntr = g->ntraces;
-  SEMB_TRY(dev_alloc(&pl->d_samples, (size_t)ntr * pl->pitch));
+  SEMB_TRY(dev_reuse(pl, &pl->d_samples, (size_t)ntr * pl->pitch));
   SEMB_CUDA(cudaMemsetAsync(pl->d_samples, 0, (size_t)ntr * pl->pitch * sizeof(float), st));
   SEMB_CUDA(cudaMemcpy2DAsync(pl->d_samples, pl->pitch * sizeof(float), g->samples, (size_t)g->ns * sizeof(float),
                               (size_t)g->ns * sizeof(float), (size_t)ntr, cudaMemcpyHostToDevice, st));
@@ -610,7 +635,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
 
   // neighbour lists: CRS from midpoints within apm, CMP the CDP itself
   const int nc_blocks = (g->ncdps + 255) / 256;
-  SEMB_TRY(dev_alloc(&pl->d_nbr_off, g->ncdps + 1));
+  SEMB_TRY(dev_reuse(pl, &pl->d_nbr_off, g->ncdps + 1));
   if (p.method == SEMB_CRS) {
     k_cdp_midpoints<<<nc_blocks, 256, 0, st>>>(g->ncdps, d_cdp_end, d_gx, d_gy, d_sx, d_sy, d_sc, d_fmx, d_fmy);
     if (g->ncdps >= kGridNeighbours) {
@@ -639,16 +664,16 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   SEMB_CUDA(cudaGetLastError());
 
   // aperture lists
-  SEMB_TRY(dev_alloc(&pl->d_ap_off, g->ncdps + 1));
+  SEMB_TRY(dev_reuse(pl, &pl->d_ap_off, g->ncdps + 1));
   k_aperture_count<<<nc_blocks, 256, 0, st>>>(g->ncdps, pl->d_nbr_off, pl->d_nbr, d_cdp_end, d_cnt64);
   k_scan_exclusive<int64_t><<<1, 1024, 0, st>>>(g->ncdps, d_cnt64, pl->d_ap_off);
   std::vector<int64_t> ap_off(g->ncdps + 1);
   SEMB_CUDA(cudaMemcpyAsync(ap_off.data(), pl->d_ap_off, ap_off.size() * 8, cudaMemcpyDeviceToHost, st));
   SEMB_CUDA(cudaStreamSynchronize(st));
   pl->nap = ap_off[g->ncdps];
-  SEMB_TRY(dev_alloc(&pl->d_ap_tr, pl->nap));
-  SEMB_TRY(dev_alloc(&pl->d_ap_geo, pl->nap));
-  SEMB_TRY(dev_alloc(&pl->d_ap_geo64, pl->nap));
+  SEMB_TRY(dev_reuse(pl, &pl->d_ap_tr, pl->nap));
+  SEMB_TRY(dev_reuse(pl, &pl->d_ap_geo, pl->nap));
+  SEMB_TRY(dev_reuse(pl, &pl->d_ap_geo64, pl->nap));
   // azimuth direction for the signed midpoint displacement (SEMB_DM_SIGNED)
   const double az = p.azimuth * 3.14159265358979323846 / 180.0;
   const double cos_d = std::cos(az), sin_d = std::sin(az);
@@ -664,8 +689,8 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
 
   // 16-bit store (batched form)
   if (p.mode == SEMB_BATCHED && p.storage != SEMB_STORE_F32) {
-    SEMB_TRY(dev_alloc(&pl->d_samples16, (size_t)ntr * pl->pitch));
-    SEMB_TRY(dev_alloc(&pl->d_scale, ntr));
+    SEMB_TRY(dev_reuse(pl, &pl->d_samples16, (size_t)ntr * pl->pitch));
+    SEMB_TRY(dev_reuse(pl, &pl->d_scale, ntr));
     k_make_store16<<<(int)std::min<int64_t>(ntr, 65535), 256, 0, st>>>(ntr, g->ns, pl->pitch, p.storage,
                                                                        pl->d_samples, pl->d_samples16, pl->d_scale);
     SEMB_CUDA(cudaGetLastError());
@@ -708,7 +733,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   for (int c : cdp_order)
     for (int b = 0; b < nblk; ++b) tasks[q++] = make_int2(c, b * kTB);
   pl->ntasks = (int)ntasks;
-  SEMB_TRY(dev_alloc(&pl->d_tasks, tasks.size()));
+  SEMB_TRY(dev_reuse(pl, &pl->d_tasks, tasks.size()));
   SEMB_CUDA(cudaMemcpyAsync(pl->d_tasks, tasks.data(), tasks.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
 
   // aperture buckets (batched form): contiguous ranges of the sorted queue split at
@@ -749,15 +774,15 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
 
   // outputs
   const size_t nout = (size_t)g->ncdps * g->ns;
-  SEMB_TRY(dev_alloc(&pl->d_ctr, nout));
-  SEMB_TRY(dev_alloc(&pl->d_str, nout));
-  SEMB_TRY(dev_alloc(&pl->d_stk, nout));
-  SEMB_TRY(dev_alloc(&pl->d_stt00, g->ncdps));
+  SEMB_TRY(dev_reuse(pl, &pl->d_ctr, nout));
+  SEMB_TRY(dev_reuse(pl, &pl->d_str, nout));
+  SEMB_TRY(dev_reuse(pl, &pl->d_stk, nout));
+  SEMB_TRY(dev_reuse(pl, &pl->d_stt00, g->ncdps));
   SEMB_CUDA(cudaMemsetAsync(pl->d_stt00, 0, g->ncdps * sizeof(float), st));
   if (form == FORM_FAST) {
-    SEMB_TRY(dev_alloc(&pl->d_top_sem, nout * kTopK));
-    SEMB_TRY(dev_alloc(&pl->d_top_idx, nout * kTopK));
-    SEMB_TRY(dev_alloc(&pl->d_top_stk, nout * kTopK));
+    SEMB_TRY(dev_reuse(pl, &pl->d_top_sem, nout * kTopK));
+    SEMB_TRY(dev_reuse(pl, &pl->d_top_idx, nout * kTopK));
+    SEMB_TRY(dev_reuse(pl, &pl->d_top_stk, nout * kTopK));
     if (p.attrs) {
       SEMB_TRY(dev_alloc(&pl->d_sem2, nout));
       SEMB_TRY(dev_alloc(&pl->d_idx2, nout));

@@ -170,6 +170,32 @@ def test_reupload_and_rerun_are_stable():
         assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("mode", [semb.PLAIN_F32, semb.BATCHED])
+def test_reupload_of_other_surveys_reuses_buffers_safely(mode):
+    """One plan uploads a large, a small and the large survey again (the device
+    buffers of the first are kept and reused): each result equals a fresh plan's."""
+    meta_a, _, _, path_a = G.load("crs_uneven_w5")
+    meta_b, _, _, path_b = G.load("crs_line")
+    pa, pb = meta_a["params"], meta_b["params"]
+    sva = semb.Survey.load(path_a, semb.CRS, pa["aph"])
+    svb = semb.Survey.load(path_b, semb.CRS, pa["aph"])
+
+    def fresh(sv):
+        with semb.Plan(semb.params(semb.CRS, mode=mode, **pa)) as q:
+            q.upload(sv.view())
+            q.run()
+            return q.download()
+
+    ref_a, ref_b = fresh(sva), fresh(svb)
+    with semb.Plan(semb.params(semb.CRS, mode=mode, **pa)) as plan:
+        for sv, ref in ((sva, ref_a), (svb, ref_b), (sva, ref_a)):
+            plan.upload(sv.view())
+            plan.run()
+            out = plan.download()
+            for x, y in zip(out, ref):
+                assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("case", ["cmp_line", "cmp_uneven_w1", "cmp_farout", "crs_line", "crs_uneven_w5"])
 def test_every_variant_agrees_with_the_default(case):
     """Each search-kernel variant (items per thread, CTAs per SM, staging and
