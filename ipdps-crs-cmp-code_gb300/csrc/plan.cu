@@ -77,6 +77,8 @@ struct semb_plan {
   semb_params p{};
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;   // upload: the trace copy and store build
+  cudaEvent_t copy_done = nullptr;
   int sms = 0;
   bool uploaded = false;
 
@@ -96,6 +98,7 @@ struct semb_plan {
 
   // device buffers
   float* d_samples = nullptr;
+  float* d_packed = nullptr;   // host layout of the traces, the upload's landing buffer
   uint16_t* d_samples16 = nullptr;
   float* d_scale = nullptr;
   int64_t* d_ap_off = nullptr;
@@ -204,6 +207,7 @@ void free_data(semb_plan* pl, bool keep_reusable = false) {
     dev_free(ptr);
   };
   release(pl->d_samples);
+  release(pl->d_packed);
   release(pl->d_samples16);
   release(pl->d_scale);
   release(pl->d_ap_off);
@@ -512,6 +516,8 @@ int semb_plan_create(const semb_params* p, int32_t device, semb_plan** out) {
   cudaDeviceProp prop;
   cudaError_t e = cudaGetDeviceProperties(&prop, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->copy_done, cudaEventDisableTiming);
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&pl->ev[i]);
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_status, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_counter, kMaxBuckets * sizeof(int));
@@ -540,6 +546,9 @@ int semb_plan_destroy(semb_plan* pl) {
   dev_free(pl->d_repicked);
   for (auto& ev : pl->ev)
     if (ev) cudaEventDestroy(ev);
+  if (pl->copy_stream) cudaStreamSynchronize(pl->copy_stream);
+  if (pl->copy_done) cudaEventDestroy(pl->copy_done);
+  if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
   if (pl->stream) cudaStreamDestroy(pl->stream);
   delete pl;
   return SEMB_OK;
@@ -592,10 +601,34 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   cudaEventRecord(pl->ev[4], st);
   // trace store
   const int64_t ntr = g->ntraces;
+  // the traces go on the copy stream, overlapped with the geometry and aperture
+  // set-up on the plan's stream: one contiguous host-to-device copy of the packed
+  // traces (a single large transfer instead of one row per trace), then the pitched
+  // store with its zero padding and, batched, the 16-bit store, on the device
+  cudaStream_t cs = pl->copy_stream;
+  struct CopyJoin {   // every exit waits for the copies, which read the caller's buffer
+    cudaStream_t s;
+    ~CopyJoin() { cudaStreamSynchronize(s); }
+  } copy_join{cs};
+  SEMB_CUDA(cudaStreamWaitEvent(cs, pl->ev[4], 0));
   SEMB_TRY(dev_reuse(pl, &pl->d_samples, (size_t)ntr * pl->pitch));
-  SEMB_CUDA(cudaMemsetAsync(pl->d_samples, 0, (size_t)ntr * pl->pitch * sizeof(float), st));
-  SEMB_CUDA(cudaMemcpy2DAsync(pl->d_samples, pl->pitch * sizeof(float), g->samples, (size_t)g->ns * sizeof(float),
-                              (size_t)g->ns * sizeof(float), (size_t)ntr, cudaMemcpyHostToDevice, st));
+  SEMB_TRY(dev_reuse(pl, &pl->d_packed, (size_t)ntr * g->ns));
+  SEMB_CUDA(cudaMemcpyAsync(pl->d_packed, g->samples, (size_t)ntr * g->ns * sizeof(float), cudaMemcpyHostToDevice,
+                            cs));
+  {
+    const int64_t groups = ntr * (pl->pitch / 4);
+    const int blocks = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)pl->sms * 32);
+    k_repitch<<<blocks, 256, 0, cs>>>(ntr, g->ns, pl->pitch, pl->d_packed, pl->d_samples);
+    SEMB_CUDA(cudaGetLastError());
+  }
+  if (p.mode == SEMB_BATCHED && p.storage != SEMB_STORE_F32) {
+    SEMB_TRY(dev_reuse(pl, &pl->d_samples16, (size_t)ntr * pl->pitch));
+    SEMB_TRY(dev_reuse(pl, &pl->d_scale, ntr));
+    k_make_store16<<<(int)std::min<int64_t>(ntr, 65535), 256, 0, cs>>>(ntr, g->ns, pl->pitch, p.storage,
+                                                                       pl->d_samples, pl->d_samples16, pl->d_scale);
+    SEMB_CUDA(cudaGetLastError());
+  }
+  SEMB_CUDA(cudaEventRecord(pl->copy_done, cs));
 
   // header fields and CDP ranges (scratch for the set-up kernels)
   int32_t *d_gx, *d_gy, *d_sx, *d_sy, *d_sc;
@@ -686,15 +719,6 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   int max_ap = 0;
   for (int i = 0; i < g->ncdps; ++i) max_ap = std::max<int64_t>(max_ap, ap_off[i + 1] - ap_off[i]);
   pl->max_ap = max_ap;
-
-  // 16-bit store (batched form)
-  if (p.mode == SEMB_BATCHED && p.storage != SEMB_STORE_F32) {
-    SEMB_TRY(dev_reuse(pl, &pl->d_samples16, (size_t)ntr * pl->pitch));
-    SEMB_TRY(dev_reuse(pl, &pl->d_scale, ntr));
-    k_make_store16<<<(int)std::min<int64_t>(ntr, 65535), 256, 0, st>>>(ntr, g->ns, pl->pitch, p.storage,
-                                                                       pl->d_samples, pl->d_samples16, pl->d_scale);
-    SEMB_CUDA(cudaGetLastError());
-  }
 
   // candidate grid and search order
   grid_f32(p, pl->ga, pl->gb, pl->gc);
@@ -808,6 +832,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
 
   // the default variant of this method and window; variant 0 where it does not fit
   if (set_all(pl, default_variant(p.method, form, pl->w)) != SEMB_OK) SEMB_TRY(set_all(pl, 0));
+  SEMB_CUDA(cudaStreamWaitEvent(st, pl->copy_done, 0));   // the stores are complete for the run
   cudaEventRecord(pl->ev[5], st);
   SEMB_CUDA(cudaStreamSynchronize(st));
   float ms = 0.f;
