@@ -281,7 +281,8 @@ def run_ours(args, rank, world, dist):
         return float(t.item())
 
     storage = {"f16": semb.STORE_F16, "bf16": semb.STORE_BF16, "f32": semb.STORE_F32}[args.storage]
-    plan = semb.Plan(semb.params(method, mode=semb.BATCHED, storage=storage, **s.params), device=dev)
+    gap = {} if args.repick_gap is None else {"repick_gap": args.repick_gap}
+    plan = semb.Plan(semb.params(method, mode=semb.BATCHED, storage=storage, **gap, **s.params), device=dev)
     plan.upload(arrays.view())
     tune = plan.autotune() if args.tune else None
     buckets = plan.buckets()
@@ -448,6 +449,8 @@ def main():
     ap.add_argument("--tune", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--repick-gap", type=float, default=None,
+                    help="near-tie threshold of the FP64 re-pick (default: the library's)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true")
     args = ap.parse_args()
