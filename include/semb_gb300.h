@@ -105,7 +105,7 @@ typedef struct semb_params {
 } semb_params;
 
 /* Fill `p` with the defaults for `method` (grid fields zero, batched FP16 with
- * near-tie re-pick at gap 3e-4).  Replaces nothing in the reference. */
+ * near-tie re-pick at gap 1e-4).  Replaces nothing in the reference. */
 void semb_params_init(semb_params* p, int32_t method);
 
 /* A linearized gather: what su_gather::linearize hands to the search

@@ -98,7 +98,6 @@ struct semb_plan {
 
   // device buffers
   float* d_samples = nullptr;
-  float* d_packed = nullptr;   // host layout of the traces, the upload's landing buffer
   uint16_t* d_samples16 = nullptr;
   float* d_scale = nullptr;
   int64_t* d_ap_off = nullptr;
@@ -207,7 +206,6 @@ void free_data(semb_plan* pl, bool keep_reusable = false) {
     dev_free(ptr);
   };
   release(pl->d_samples);
-  release(pl->d_packed);
   release(pl->d_samples16);
   release(pl->d_scale);
   release(pl->d_ap_off);
@@ -602,9 +600,8 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   // trace store
   const int64_t ntr = g->ntraces;
   // the traces go on the copy stream, overlapped with the geometry and aperture
-  // set-up on the plan's stream: one contiguous host-to-device copy of the packed
-  // traces (a single large transfer instead of one row per trace), then the pitched
-  // store with its zero padding and, batched, the 16-bit store, on the device
+  // set-up on the plan's stream: the pitched store (zero padding, rows copied by one
+  // 2-D transfer) and, batched, the 16-bit store built from it on the device
   cudaStream_t cs = pl->copy_stream;
   struct CopyJoin {   // every exit waits for the copies, which read the caller's buffer
     cudaStream_t s;
@@ -612,15 +609,9 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   } copy_join{cs};
   SEMB_CUDA(cudaStreamWaitEvent(cs, pl->ev[4], 0));
   SEMB_TRY(dev_reuse(pl, &pl->d_samples, (size_t)ntr * pl->pitch));
-  SEMB_TRY(dev_reuse(pl, &pl->d_packed, (size_t)ntr * g->ns));
-  SEMB_CUDA(cudaMemcpyAsync(pl->d_packed, g->samples, (size_t)ntr * g->ns * sizeof(float), cudaMemcpyHostToDevice,
-                            cs));
-  {
-    const int64_t groups = ntr * (pl->pitch / 4);
-    const int blocks = (int)std::min<int64_t>((groups + 255) / 256, (int64_t)pl->sms * 32);
-    k_repitch<<<blocks, 256, 0, cs>>>(ntr, g->ns, pl->pitch, pl->d_packed, pl->d_samples);
-    SEMB_CUDA(cudaGetLastError());
-  }
+  SEMB_CUDA(cudaMemsetAsync(pl->d_samples, 0, (size_t)ntr * pl->pitch * sizeof(float), cs));
+  SEMB_CUDA(cudaMemcpy2DAsync(pl->d_samples, pl->pitch * sizeof(float), g->samples, (size_t)g->ns * sizeof(float),
+                              (size_t)g->ns * sizeof(float), (size_t)ntr, cudaMemcpyHostToDevice, cs));
   if (p.mode == SEMB_BATCHED && p.storage != SEMB_STORE_F32) {
     SEMB_TRY(dev_reuse(pl, &pl->d_samples16, (size_t)ntr * pl->pitch));
     SEMB_TRY(dev_reuse(pl, &pl->d_scale, ntr));

@@ -208,25 +208,6 @@ static __global__ void k_aperture_fill(int ncdps, int method, const int64_t* __r
 
 // 16-bit trace store: per trace, scale = max|s| / 32768 (1 for an all-zero trace)
 // and s16 = s / scale rounded to nearest.  One block per trace.
-// Packed traces [ntr][ns] (as copied from the host in one contiguous transfer) into
-// the pitched store [ntr][pitch], zeros after each trace's last sample.  Grid-stride
-// over 16-byte groups of the pitched store (pitch is a multiple of 8 floats).
-static __global__ void k_repitch(int64_t ntr, int ns, int64_t pitch, const float* __restrict__ packed,
-                                 float* __restrict__ pitched) {
-  const int64_t groups = ntr * (pitch / 4);
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < groups; q += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t tr = q / (pitch / 4);
-    const int k = (int)(q - tr * (pitch / 4)) * 4;
-    const float* src = packed + tr * ns;
-    float4 v;
-    v.x = k < ns ? src[k] : 0.f;
-    v.y = k + 1 < ns ? src[k + 1] : 0.f;
-    v.z = k + 2 < ns ? src[k + 2] : 0.f;
-    v.w = k + 3 < ns ? src[k + 3] : 0.f;
-    reinterpret_cast<float4*>(pitched + tr * pitch)[k / 4] = v;
-  }
-}
-
 static __global__ void k_make_store16(int64_t ntr, int ns, int64_t pitch, int storage, const float* __restrict__ s32,
                                uint16_t* __restrict__ s16, float* __restrict__ scale) {
   __shared__ float red[32];

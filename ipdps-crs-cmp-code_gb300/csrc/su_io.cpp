@@ -204,7 +204,7 @@ void semb_params_init(semb_params* p, int32_t method) {
   p->mode = SEMB_BATCHED;
   p->storage = SEMB_STORE_F16;
   p->repick = SEMB_REPICK_NEAR_TIES;
-  p->repick_gap = 3e-4f;
+  p->repick_gap = 1e-4f;
   p->na = p->nb = 1;
 }
 

@@ -151,7 +151,7 @@ def _ptr(a: np.ndarray | None):
 
 
 def params(method: int, mode: int = PLAIN_F32, storage: int = STORE_F16, repick: int = REPICK_NEAR_TIES,
-           repick_gap: float = 3e-4, dm_mode: int = DM_ABS, attrs: int = 0, ngen: int = 0,
+           repick_gap: float = 1e-4, dm_mode: int = DM_ABS, attrs: int = 0, ngen: int = 0,
            **kw) -> SembParams:
     """Build semb_params from the reference's flag names (c0, c1, nc, aph, tau, and
     for CRS a0, a1, na, b0, b1, nb, apm, azimuth).  CMP values are rounded to float

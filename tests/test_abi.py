@@ -37,7 +37,7 @@ def test_params_defaults(semb_lib):
     p = semb.params(semb.CRS)
     assert p.method == semb.CRS and p.mode == semb.PLAIN_F32
     assert p.storage == semb.STORE_F16 and p.repick == semb.REPICK_NEAR_TIES
-    assert abs(p.repick_gap - 3e-4) < 1e-9
+    assert abs(p.repick_gap - 1e-4) < 1e-9
 
 
 def test_cmp_params_are_rounded_like_stof(semb_lib):
