@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 6
+#define SEMB_ABI_VERSION 7
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
 #define SEMB_MAX_VARIANTS 16
@@ -197,6 +197,16 @@ int semb_plan_upload(semb_plan* plan, const semb_gather_view* g);
  * and the CUDA kernels compute_semblances + redux_semblances
  * (CMP/CUDA/src/main.cu:87-173, CRS/CUDA/src/main.cu:154-264).  Synchronous. */
 int semb_plan_run(semb_plan* plan);
+
+/* Upload and search in one call, streamed (batched grid search): the gather's CDPs
+ * are cut into nchunks (1..64) contiguous chunks of about equal trace counts; the
+ * traces of each chunk are copied to the device while the search of the chunks
+ * whose apertures have landed runs, so the host-to-device transfer overlaps the
+ * search.  Results as semb_plan_upload + semb_plan_run (same queue per chunk, longest
+ * aperture first); the plan is then uploaded as by semb_plan_upload.  Synchronous;
+ * the gather's memory must stay valid until it returns.  No counterpart in the
+ * reference, which reads, copies and searches CDP by CDP. */
+int semb_plan_stream(semb_plan* plan, const semb_gather_view* gather, int32_t nchunks);
 
 /* Copy the results to host arrays of ncdps*ns elements, CDP-major in the gather's
  * CDP order: ctr = picked candidate index (CMP: -1 when no candidate has positive

@@ -131,6 +131,15 @@ struct semb_plan {
   float* d_de_b = nullptr;
   float* d_de_c = nullptr;
 
+  // streamed upload (semb_plan_stream): CDP chunks whose traces are copied while
+  // the search of earlier chunks runs
+  int nchunks = 0;
+  std::vector<int> chunk_cdp;    // [nchunks+1] CDP boundaries
+  std::vector<int> chunk_task;   // [nchunks+1] boundaries in the task queue
+  std::vector<int> chunk_need;   // the last chunk whose traces chunk k's apertures read
+  std::vector<cudaEvent_t> chunk_done;
+  int* d_chunk_counter = nullptr;
+
   // bytes held by each buffer that a later upload of the same size reuses
   std::unordered_map<const void*, size_t> caps;
 
@@ -545,6 +554,8 @@ int semb_plan_destroy(semb_plan* pl) {
   for (auto& ev : pl->ev)
     if (ev) cudaEventDestroy(ev);
   if (pl->copy_stream) cudaStreamSynchronize(pl->copy_stream);
+  for (cudaEvent_t e : pl->chunk_done) cudaEventDestroy(e);
+  dev_free(pl->d_chunk_counter);
   if (pl->copy_done) cudaEventDestroy(pl->copy_done);
   if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
   if (pl->stream) cudaStreamDestroy(pl->stream);
@@ -552,7 +563,46 @@ int semb_plan_destroy(semb_plan* pl) {
   return SEMB_OK;
 }
 
-int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
+namespace {
+int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks);
+int enqueue_streamed(semb_plan* pl, const semb_gather_view* g);
+int enqueue_repick(semb_plan* pl, cudaStream_t st);
+}  // namespace
+
+int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) { return upload_impl(pl, g, 0); }
+
+int semb_plan_stream(semb_plan* pl, const semb_gather_view* g, int32_t nchunks) {
+  if (!pl || !g) return fail(SEMB_E_ARG, "null argument");
+  if (pl->p.mode != SEMB_BATCHED || pl->p.ngen > 0)
+    return fail(SEMB_E_ARG, "the streamed search is the batched form's grid search");
+  if (nchunks < 1 || nchunks > 64) return fail(SEMB_E_ARG, "nchunks must be in 1..64");
+  SEMB_TRY(upload_impl(pl, g, nchunks));
+  return enqueue_streamed(pl, g);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Traces [t0, t1) of the gather into the device stores on stream cs: the pitched
+// FP32 rows with their zero padding (one 2-D copy) and, batched, the 16-bit rows.
+int copy_traces(semb_plan* pl, const semb_gather_view* g, int64_t t0, int64_t t1, cudaStream_t cs) {
+  const int64_t n = t1 - t0;
+  if (n <= 0) return SEMB_OK;
+  float* dst = pl->d_samples + t0 * pl->pitch;
+  SEMB_CUDA(cudaMemsetAsync(dst, 0, (size_t)n * pl->pitch * sizeof(float), cs));
+  SEMB_CUDA(cudaMemcpy2DAsync(dst, pl->pitch * sizeof(float), g->samples + t0 * g->ns, (size_t)g->ns * sizeof(float),
+                              (size_t)g->ns * sizeof(float), (size_t)n, cudaMemcpyHostToDevice, cs));
+  if (pl->p.mode == SEMB_BATCHED && pl->p.storage != SEMB_STORE_F32) {
+    k_make_store16<<<(int)std::min<int64_t>(n, 65535), 256, 0, cs>>>(n, g->ns, pl->pitch, pl->p.storage, dst,
+                                                                     pl->d_samples16 + t0 * pl->pitch,
+                                                                     pl->d_scale + t0);
+    SEMB_CUDA(cudaGetLastError());
+  }
+  return SEMB_OK;
+}
+
+int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   if (!pl || !g) return fail(SEMB_E_ARG, "null argument");
   const semb_params& p = pl->p;
   if (g->ncdps <= 0 || g->ns <= 0 || g->ntraces <= 0 || !g->cdp_end || !g->gx || !g->gy || !g->sx || !g->sy ||
@@ -609,16 +659,11 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   } copy_join{cs};
   SEMB_CUDA(cudaStreamWaitEvent(cs, pl->ev[4], 0));
   SEMB_TRY(dev_reuse(pl, &pl->d_samples, (size_t)ntr * pl->pitch));
-  SEMB_CUDA(cudaMemsetAsync(pl->d_samples, 0, (size_t)ntr * pl->pitch * sizeof(float), cs));
-  SEMB_CUDA(cudaMemcpy2DAsync(pl->d_samples, pl->pitch * sizeof(float), g->samples, (size_t)g->ns * sizeof(float),
-                              (size_t)g->ns * sizeof(float), (size_t)ntr, cudaMemcpyHostToDevice, cs));
   if (p.mode == SEMB_BATCHED && p.storage != SEMB_STORE_F32) {
     SEMB_TRY(dev_reuse(pl, &pl->d_samples16, (size_t)ntr * pl->pitch));
     SEMB_TRY(dev_reuse(pl, &pl->d_scale, ntr));
-    k_make_store16<<<(int)std::min<int64_t>(ntr, 65535), 256, 0, cs>>>(ntr, g->ns, pl->pitch, p.storage,
-                                                                       pl->d_samples, pl->d_samples16, pl->d_scale);
-    SEMB_CUDA(cudaGetLastError());
   }
+  if (nchunks == 0) SEMB_TRY(copy_traces(pl, g, 0, ntr, cs));   // streamed: per chunk in the run
   SEMB_CUDA(cudaEventRecord(pl->copy_done, cs));
 
   // header fields and CDP ranges (scratch for the set-up kernels)
@@ -745,8 +790,48 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   if (ntasks >= INT32_MAX) return fail(SEMB_E_ARG, "too many tasks");
   std::vector<int2> tasks((size_t)ntasks);
   size_t q = 0;
-  for (int c : cdp_order)
-    for (int b = 0; b < nblk; ++b) tasks[q++] = make_int2(c, b * kTB);
+  pl->nchunks = nchunks;
+  if (nchunks == 0) {
+    for (int c : cdp_order)
+      for (int b = 0; b < nblk; ++b) tasks[q++] = make_int2(c, b * kTB);
+  } else {
+    // streamed: CDP chunks of about equal trace counts in gather order, each chunk's
+    // tasks longest aperture first; chunk k's search waits for the copies of the
+    // last chunk its apertures read (chunk_need)
+    pl->chunk_cdp.assign(1, 0);
+    for (int k = 1; k < nchunks; ++k) {
+      const int64_t target = g->ntraces * k / nchunks;
+      int c = pl->chunk_cdp.back();
+      while (c < g->ncdps && g->cdp_end[c] <= target) ++c;
+      pl->chunk_cdp.push_back(std::max(c, pl->chunk_cdp.back()));
+    }
+    pl->chunk_cdp.push_back(g->ncdps);
+    std::vector<int> chunk_of(g->ncdps);
+    for (int k = 0; k < nchunks; ++k)
+      for (int c = pl->chunk_cdp[k]; c < pl->chunk_cdp[k + 1]; ++c) chunk_of[c] = k;
+    std::vector<int64_t> noff(g->ncdps + 1);
+    std::vector<int32_t> nlist((size_t)std::max<int64_t>(pl->n_nbr, 1));
+    SEMB_CUDA(cudaMemcpyAsync(noff.data(), pl->d_nbr_off, noff.size() * 8, cudaMemcpyDeviceToHost, st));
+    SEMB_CUDA(cudaMemcpyAsync(nlist.data(), pl->d_nbr, (size_t)pl->n_nbr * 4, cudaMemcpyDeviceToHost, st));
+    SEMB_CUDA(cudaStreamSynchronize(st));
+    pl->chunk_need.assign(nchunks, 0);
+    pl->chunk_task.assign(1, 0);
+    for (int k = 0; k < nchunks; ++k) {
+      int need = k;
+      std::vector<int> cs_k;
+      for (int c = pl->chunk_cdp[k]; c < pl->chunk_cdp[k + 1]; ++c) {
+        cs_k.push_back(c);
+        for (int64_t e = noff[c]; e < noff[c + 1]; ++e) need = std::max(need, chunk_of[nlist[e]]);
+      }
+      pl->chunk_need[k] = need;
+      std::stable_sort(cs_k.begin(), cs_k.end(), [&](int x, int y) {
+        return ap_off[x + 1] - ap_off[x] > ap_off[y + 1] - ap_off[y];
+      });
+      for (int c : cs_k)
+        for (int b = 0; b < nblk; ++b) tasks[q++] = make_int2(c, b * kTB);
+      pl->chunk_task.push_back((int)q);
+    }
+  }
   pl->ntasks = (int)ntasks;
   SEMB_TRY(dev_reuse(pl, &pl->d_tasks, tasks.size()));
   SEMB_CUDA(cudaMemcpyAsync(pl->d_tasks, tasks.data(), tasks.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
@@ -759,7 +844,7 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
     std::vector<Bucket> bs;
     size_t t = 0;
     const size_t nt = tasks.size();
-    const int nsplit = form == FORM_FAST ? kBucketSplits : 0;
+    const int nsplit = form == FORM_FAST && nchunks == 0 ? kBucketSplits : 0;
     for (int k = 0; k <= nsplit && t < nt; ++k) {
       const int lo = k < nsplit ? kBucketAp[k] : INT32_MIN;   // bucket k holds apertures > lo
       Bucket b;
@@ -844,10 +929,6 @@ int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) {
   pl->uploaded = true;
   return SEMB_OK;
 }
-
-}  // extern "C"
-
-namespace {
 
 // Kernel parameters for configuration `cfg` over tasks[0, ntasks) with work-queue
 // head `counter`.
@@ -964,6 +1045,18 @@ int enqueue_run(semb_plan* pl, bool timed) {
   }
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
   if (form == FORM_FAST) {
+    SEMB_TRY(enqueue_repick(pl, st));
+    ++launches;
+  }
+  if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
+  pl->stats.kernel_launches = launches;
+  return SEMB_OK;
+}
+
+// The FP64 near-tie re-pick of the batched form, on stream st.
+int enqueue_repick(semb_plan* pl, cudaStream_t st) {
+  const semb_params& p = pl->p;
+  {
     RepickParams R{};
     R.top_sem = pl->d_top_sem;
     R.top_idx = pl->d_top_idx;
@@ -992,10 +1085,72 @@ int enqueue_run(semb_plan* pl, bool timed) {
     R.err64 = pl->d_err64;
     SEMB_CUDA(cudaMemsetAsync(pl->d_repicked, 0, sizeof(unsigned long long), st));
     SEMB_TRY(launch_repick(pl->w, R, st));
+  }
+  return SEMB_OK;
+}
+
+// Streamed search (semb_plan_stream): the traces of chunk k are copied on the copy
+// stream while the plan's stream searches the chunks whose apertures have landed;
+// then the CRS t0 = 0 stacks and the re-pick.  Synchronous, like semb_plan_run.
+int enqueue_streamed(semb_plan* pl, const semb_gather_view* g) {
+  cudaStream_t st = pl->stream, cs = pl->copy_stream;
+  const semb_params& p = pl->p;
+  struct CopyJoin {
+    cudaStream_t s;
+    ~CopyJoin() { cudaStreamSynchronize(s); }
+  } join{cs};
+  const int nk = pl->nchunks;
+  while ((int)pl->chunk_done.size() < nk) {
+    cudaEvent_t e;
+    SEMB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    pl->chunk_done.push_back(e);
+  }
+  SEMB_TRY(dev_reuse(pl, &pl->d_chunk_counter, nk));
+  SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, sizeof(int), st));
+  SEMB_CUDA(cudaMemsetAsync(pl->d_chunk_counter, 0, nk * sizeof(int), st));
+  SEMB_CUDA(cudaEventRecord(pl->ev[0], st));
+  SEMB_CUDA(cudaStreamWaitEvent(cs, pl->ev[0], 0));
+  for (int k = 0; k < nk; ++k) {
+    const int c0 = pl->chunk_cdp[k], c1 = pl->chunk_cdp[k + 1];
+    const int64_t t0 = c0 > 0 ? g->cdp_end[c0 - 1] : 0, t1 = c1 > 0 ? g->cdp_end[c1 - 1] : 0;
+    SEMB_TRY(copy_traces(pl, g, t0, t1, cs));
+    SEMB_CUDA(cudaEventRecord(pl->chunk_done[k], cs));
+  }
+  const Bucket& b = pl->buckets[0];
+  const int form = FORM_FAST;
+  int launches = 0;
+  for (int k = 0; k < nk; ++k) {
+    const int n = pl->chunk_task[k + 1] - pl->chunk_task[k];
+    if (n == 0) continue;
+    SEMB_CUDA(cudaStreamWaitEvent(st, pl->chunk_done[pl->chunk_need[k]], 0));
+    const KParams P = make_kparams_cfg(pl, b.cfg, pl->d_tasks + pl->chunk_task[k], n, pl->d_chunk_counter + k);
+    SEMB_TRY(launch_search(p.method, form, pl->w, b.cfg.variant, P, b.cfg.nwarps, std::min(n, pl->sms * b.cfg.occ),
+                           b.cfg.smem, st));
     ++launches;
   }
-  if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
+  SEMB_CUDA(cudaStreamWaitEvent(st, pl->chunk_done[nk - 1], 0));
+  if (p.method == SEMB_CRS) {
+    const KParams P = make_kparams(pl, 0);
+    SEMB_TRY(launch_stt00(pl->w, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
+    ++launches;
+  }
+  SEMB_TRY(enqueue_repick(pl, st));
+  ++launches;
+  SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
+  SEMB_CUDA(cudaStreamSynchronize(st));
+  int status = 0;
+  unsigned long long rep = 0;
+  SEMB_CUDA(cudaMemcpy(&status, pl->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  SEMB_CUDA(cudaMemcpy(&rep, pl->d_repicked, sizeof(rep), cudaMemcpyDeviceToHost));
+  float ms = 0.f;
+  SEMB_CUDA(cudaEventElapsedTime(&ms, pl->ev[0], pl->ev[3]));
+  pl->stats.ms_search = 0.f;
+  pl->stats.ms_repick = 0.f;
+  pl->stats.ms_total = ms;
+  pl->stats.repicked = (int64_t)rep;
   pl->stats.kernel_launches = launches;
+  if (status & ST_TIMEOUT) return fail(SEMB_E_TIMEOUT, "a staging wait in the search kernel timed out");
+  if (status) return fail(SEMB_E_CUDA, "search kernel reported status %d", status);
   return SEMB_OK;
 }
 

@@ -29,7 +29,7 @@ PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
 DM_ABS, DM_SIGNED = 0, 1
-ABI_VERSION = 6
+ABI_VERSION = 7
 MAX_VARIANTS = 16   # SEMB_MAX_VARIANTS
 MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
@@ -37,7 +37,7 @@ OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODE
 
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
-    "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_run", "semb_plan_download",
+    "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_stream", "semb_plan_run", "semb_plan_download",
     "semb_plan_download_attrs", "semb_survey_write_attr", "semb_plan_download_abc", "semb_survey_write_abc",
     "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
     "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
@@ -109,6 +109,7 @@ def lib():
         "semb_plan_create": (C.c_int, [P, i32, P]),
         "semb_plan_upload": (C.c_int, [P, P]),
         "semb_plan_run": (C.c_int, [P]),
+        "semb_plan_stream": (C.c_int, [P, P, i32]),
         "semb_plan_download": (C.c_int, [P, P, P, P]),
         "semb_plan_download_attrs": (C.c_int, [P, P, P, P, P]),
         "semb_plan_download_abc": (C.c_int, [P, P, P, P]),
@@ -285,6 +286,12 @@ class Plan:
 
     def upload(self, view: SembGatherView) -> None:
         _check(lib().semb_plan_upload(self._h, C.byref(view)), "semb_plan_upload")
+        self.ncdps, self.ns = view.ncdps, view.ns
+
+    def stream(self, view: SembGatherView, nchunks: int = 4) -> None:
+        """Upload and search in one call, the trace copies of CDP chunks overlapped
+        with the search of earlier chunks (batched form)."""
+        _check(lib().semb_plan_stream(self._h, C.byref(view), int(nchunks)), "semb_plan_stream")
         self.ncdps, self.ns = view.ncdps, view.ns
 
     def run(self) -> None:

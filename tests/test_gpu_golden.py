@@ -196,6 +196,27 @@ def test_reupload_of_other_surveys_reuses_buffers_safely(mode):
                 assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("case", ["cmp_uneven_w1", "crs_line", "crs_uneven_w5"])
+@pytest.mark.parametrize("nchunks", [1, 3, 7])
+def test_streamed_search_equals_upload_and_run(case, nchunks):
+    """semb_plan_stream (chunked trace copies overlapped with the search of chunks
+    whose apertures, halos included, have landed) gives the upload + run results."""
+    meta, h, s, path = G.load(case)
+    method, p = meta["method"], meta["params"]
+    sv = semb.Survey.load(path, METHOD[method], p["aph"])
+    with semb.Plan(semb.params(METHOD[method], mode=semb.BATCHED, **p)) as plan:
+        plan.upload(sv.view())
+        plan.run()
+        ref = plan.download()
+        plan.stream(sv.view(), nchunks)
+        out = plan.download()
+        for x, y in zip(out, ref):
+            assert np.array_equal(x, y)
+        plan.run()   # the plan is uploaded afterwards
+        for x, y in zip(plan.download(), ref):
+            assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("case", ["cmp_line", "cmp_uneven_w1", "cmp_farout", "crs_line", "crs_uneven_w5"])
 def test_every_variant_agrees_with_the_default(case):
     """Each search-kernel variant (items per thread, CTAs per SM, staging and
