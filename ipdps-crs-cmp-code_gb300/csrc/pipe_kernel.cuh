@@ -91,11 +91,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// TMODE: how an in-range item splits t into sample index and weight.  0: t + 2^23
-// rounded toward zero (the index in the low mantissa bits), FP32 pipe; 1: floor to
-// int and back with the conversion unit (F2I/I2F), which leaves two FP32 ops per
-// item to the FMA pipes.  Both are exact (t > 0 in range), so results are the same.
-template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TMODE = 0>
+template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT>
 __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT, LAY);
@@ -337,19 +333,10 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
             t2 = __ffma2_rn(u, u, __ffma2_rn(cb2[rp], gy2, __fmul2_rn(cc2[rp], gz2)));
           }
           const float2 t = make_float2(sqrt_fast(t2.x), sqrt_fast(t2.y));
-          if constexpr (TMODE == 0) {
-            const float2 y = __fadd2_rz(t, kTwo23x2);
-            const float2 x = __ffma2_rn(__fadd2_rn(y, kMinusTwo23x2), kMinusOne2, t);   // t - floor(t)
-            fa[2 * rp].add(min(__float_as_uint(y.x) * EB + base, top), x.x);
-            if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * EB + base, top), x.y);
-          } else {
-            const int i0 = __float2int_rd(t.x), i1 = __float2int_rd(t.y);
-            const float2 fi = make_float2(__int2float_rn(i0), __int2float_rn(i1));
-            const float2 x = __ffma2_rn(fi, kMinusOne2, t);   // t - floor(t)
-            const uint32_t base_i = base + EB * 0x4B000000u;
-            fa[2 * rp].add(min((uint32_t)i0 * EB + base_i, top), x.x);
-            if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min((uint32_t)i1 * EB + base_i, top), x.y);
-          }
+          const float2 y = __fadd2_rz(t, kTwo23x2);
+          const float2 x = __ffma2_rn(__fadd2_rn(y, kMinusTwo23x2), kMinusOne2, t);   // t - floor(t)
+          fa[2 * rp].add(min(__float_as_uint(y.x) * EB + base, top), x.x);
+          if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * EB + base, top), x.y);
         }
       }
       // the other traces: per-item range checks; an out-of-range item reads the

@@ -39,10 +39,9 @@ SearchEntry entry() {
   return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 0, LAY};
 }
 
-template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256, int TMODE = 0>
+template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256>
 SearchEntry pipe_entry() {
-  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT, TMODE>, RC, MINB, BRUN ? 1 : 0, NT, 1,
-          LAY};
+  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 1, LAY};
 }
 
 // Plain form: one variant per window.
@@ -96,7 +95,7 @@ SearchEntry search_entry(int w, int variant) {
       if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 3, 8, 2, LAY_P2, true>();
       if (variant == 11) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 12) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 1, LAY_P2, false, 512>();
-      if (variant == 13) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_P2, METHOD == METHOD_CRS, 512, 1>();
+      if (variant == 13) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_SD, METHOD == METHOD_CRS, 512>();
       if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 3, 7, 1, LAY_P2, true, 512>();
       if (variant == 15) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
       break;
@@ -113,7 +112,7 @@ SearchEntry search_entry(int w, int variant) {
       if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 5, 8, 2, LAY_P2, true>();
       if (variant == 11) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 12) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 6), 1, LAY_P2, false, 512>();
-      if (variant == 13) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_P2, METHOD == METHOD_CRS, 512, 1>();
+      if (variant == 13) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_SD, METHOD == METHOD_CRS, 512>();
       if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 5, 7, 1, LAY_P2, true, 512>();
       if (variant == 15) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
       break;
