@@ -180,6 +180,21 @@ def traffic_from_profiles(workload: str, ncdps: int, trace_evals: int):
     return float(captured) * trace_evals / src["trace_evals"]
 
 
+def smem_from_profiles(workload: str):
+    """Shared-memory load wavefronts of the search kernel, % of peak, from the ncu
+    capture summarised in profiles/ (None when no capture covers the workload)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            table = json.load(f)
+    except (OSError, ValueError):
+        return None
+    e = table.get(workload) or {}
+    src = table.get(e.get("scaled_from", ""), e)
+    if "smem_load_wavefronts_pct_of_peak" not in src:
+        return None
+    return {"load_wavefronts_pct_of_peak": src["smem_load_wavefronts_pct_of_peak"], "source": src["smem_source"]}
+
+
 def oracle_mod():
     if ORACLE_DIR not in sys.path:
         sys.path.insert(0, ORACLE_DIR)
@@ -414,6 +429,7 @@ def run_ours(args, rank, world, dist):
                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)"}
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "traffic": traffic, "traffic_unit": "DRAM bytes per search launch (ncu)", "hbm": hbm,
+            "smem": smem_from_profiles(args.workload),
             "peak_source": "measured live: semb_probe_fp32 FMA throughput",
             "flops_per_launch": flops, "launch_ms": ms_search}
     clocks = clk.summary()
