@@ -177,6 +177,7 @@ __device__ __forceinline__ bool better(float s, int i, float bs, int bi) {
 constexpr int LAY_QUAD = 0;   // (s_k, s_k+1, s_k+2, s_k+3)
 constexpr int LAY_SD = 1;     // (s_k, s_k+1 - s_k, s_k+1, s_k+2 - s_k+1)
 constexpr int LAY_P2 = 2;     // (s_k, s_k+2, s_k+1, s_k+3)
+constexpr int LAY_PD = 3;     // w = 3: (s_k, s_k+2, s_k+1 - s_k, s_k+3 - s_k+2)
 
 // bytes of one staged entry
 __host__ __device__ constexpr int lay_entry_bytes(int) { return 16; }
@@ -446,6 +447,7 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
       }
       dst[k] = LAY == LAY_SD   ? make_float4(v[0], v[1] - v[0], v[1], v[2] - v[1])
                : LAY == LAY_P2 ? make_float4(v[0], v[2], v[1], v[3])
+               : LAY == LAY_PD ? make_float4(v[0], v[2], v[1] - v[0], v[3] - v[2])
                                : make_float4(v[0], v[1], v[2], v[3]);
     }
   }
@@ -632,6 +634,45 @@ struct FastAcc<W, LAY_P2> {
       acsq = fmaf(np[i].y, np[i].y, acsq);
       lin += np[i].x + np[i].y;
     }
+  }
+};
+
+// Packed values with their differences (w = 3): entry k = (s_k, s_k+2, d_k, d_k+2),
+// d_j = s_j+1 - s_j.  Window samples 0 and 2 are one FP32x2 FMA without forming the
+// differences; sample 1 takes s_1 = s_0 + d_0 (within a rounding of the stored value)
+// and d_1 = s_2 - s_1.
+template <int W>
+struct FastAcc<W, LAY_PD> {
+  static_assert(W == 3, "the packed value/difference layout is for w = 3");
+  float2 np;     // (num_0, num_2)
+  float ns;      // num_1
+  float2 den2;   // energy of the current chunk, two partial sums
+  int M;
+
+  __device__ __forceinline__ void reset() {
+    np = make_float2(0.f, 0.f);
+    ns = 0.f;
+    den2 = make_float2(0.f, 0.f);
+    M = 0;
+  }
+  __device__ __forceinline__ void add(uint32_t a, float x) {
+    const float4 A = lds128(a);   // (s_0, s_2, d_0, d_2)
+    const float2 v = __ffma2_rn(make_float2(A.z, A.w), make_float2(x, x), make_float2(A.x, A.y));
+    np = __fadd2_rn(np, v);
+    den2 = __ffma2_rn(v, v, den2);
+    const float s1 = A.x + A.z;
+    const float v1 = fmaf(A.y - s1, x, s1);
+    ns += v1;
+    den2.x = fmaf(v1, v1, den2.x);
+  }
+  __device__ __forceinline__ float take_energy() {
+    const float e = den2.x + den2.y;
+    den2 = make_float2(0.f, 0.f);
+    return e;
+  }
+  __device__ __forceinline__ void sums(float& acsq, float& lin) const {
+    acsq = fmaf(np.x, np.x, fmaf(np.y, np.y, ns * ns));
+    lin = np.x + np.y + ns;
   }
 };
 
