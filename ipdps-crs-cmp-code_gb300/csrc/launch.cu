@@ -30,9 +30,11 @@ int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* 
 }
 
 // Variant a plan starts with (before any autotuning): for CRS the pipelined
-// 512-thread B-run kernel, the fastest on the CRS workloads measured on GB300;
-// for CMP the two-barrier kernel's variant 0.
+// 512-thread B-run kernel, the fastest on the CRS workloads measured on GB300 (with
+// the packed value/difference staging for w = 3); for CMP the two-barrier kernel's
+// variant 0.
 int default_variant(int method, int form, int w) {
+  if (method == METHOD_CRS && form == FORM_FAST && w == 3) return 13;
   if (method == METHOD_CRS && form == FORM_FAST && w <= 5) return 14;
   return 0;
 }
