@@ -91,7 +91,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT>
+// TU: unroll factor of the in-range trace loop (independent work of TU traces in
+// flight per iteration).
+template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TU = 1>
 __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT, LAY);
@@ -310,6 +312,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
       // traces on which every item is in range: traveltimes of item pairs in
       // FP32x2, address = bits(t + 2^23) * EB + base (mod 2^32), clamped to the
       // stage as a guard
+#pragma unroll TU
       for (int e = 0; e < n_in; ++e) {
         const float4 g = meta->geo[e];
         const uint32_t base = bufq_addr + EB * (uint32_t)(__float_as_int(g.w) - P.tau) - EB * 0x4B000000u;

@@ -1036,12 +1036,20 @@ int enqueue_run(semb_plan* pl, bool timed) {
   }
   if (form == FORM_FAST) SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, kMaxBuckets * sizeof(int), st));
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[1], st));
-  for (int i = 0; i < (int)pl->buckets.size(); ++i) {
-    const Bucket& b = pl->buckets[i];
-    if (b.end == b.begin) continue;
-    const KParams Pb = make_kparams(pl, i);
-    SEMB_TRY(launch_search(p.method, form, pl->w, b.cfg.variant, Pb, b.cfg.nwarps, bucket_grid(pl, b), b.cfg.smem, st));
-    ++launches;
+  // neighbouring buckets on the same variant (same launch configuration) run as one
+  // launch over their tasks, longest aperture first, on the first one's queue head
+  for (int i = 0; i < (int)pl->buckets.size();) {
+    int j = i + 1;
+    while (j < (int)pl->buckets.size() && pl->buckets[j].cfg.variant == pl->buckets[i].cfg.variant) ++j;
+    Bucket run = pl->buckets[i];
+    run.end = pl->buckets[j - 1].end;
+    if (run.end > run.begin) {
+      const KParams Pb = make_kparams_cfg(pl, run.cfg, pl->d_tasks + run.begin, run.end - run.begin, pl->d_counter + i);
+      SEMB_TRY(launch_search(p.method, form, pl->w, run.cfg.variant, Pb, run.cfg.nwarps, bucket_grid(pl, run),
+                             run.cfg.smem, st));
+      ++launches;
+    }
+    i = j;
   }
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
   if (form == FORM_FAST) {

@@ -10,7 +10,7 @@
 // layout (LAY_SD) saves one FP32 op per window sample for 50% more shared-memory
 // bytes per evaluation; the packed layout (LAY_P2) does two window samples per
 // FP32x2 instruction, and LAY_PD (w = 3) stores the pair's differences in place of
-// the odd samples.  Variants 11 and up use the pipelined kernel
+// the odd samples (its variant unrolls the in-range trace loop by two).  Variants 11 and up use the pipelined kernel
 // (semb_pipe_kernel), whose warps hand chunks over through mbarriers instead of
 // meeting at CTA barriers.  RC values keep the per-item
 // register state within 65536 / (256 * MINB) registers without spilling
@@ -40,9 +40,9 @@ SearchEntry entry() {
   return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 0, LAY};
 }
 
-template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256>
+template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256, int TU = 1>
 SearchEntry pipe_entry() {
-  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 1, LAY};
+  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT, TU>, RC, MINB, BRUN ? 1 : 0, NT, 1, LAY};
 }
 
 // Plain form: one variant per window.
@@ -96,7 +96,7 @@ SearchEntry search_entry(int w, int variant) {
       if (METHOD == METHOD_CRS && variant == 10) return entry<METHOD, FORM, 3, 8, 2, LAY_P2, true>();
       if (variant == 11) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 2>();
       if (variant == 12) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 6), 1, LAY_P2, false, 512>();
-      if (variant == 13) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 512>();
+      if (variant == 13) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 512, 2>();
       if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 3, 7, 1, LAY_P2, true, 512>();
       if (variant == 15) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
       break;

@@ -1,5 +1,6 @@
-"""Aperture buckets of the batched work queue (GPU): each bucket is its own launch
-with its own tuned variant, and the result does not depend on how the queue is split."""
+"""Aperture buckets of the batched work queue (GPU): each bucket has its own tuned
+variant (neighbours on the same variant run as one launch), and the result does not
+depend on how the queue is split."""
 import numpy as np
 import pytest
 
@@ -48,10 +49,12 @@ def test_buckets_cover_the_queue_and_tuning_keeps_the_result():
         out = plan.download()
         assert np.mean(out[0] == base[0]) >= 0.995
         np.testing.assert_allclose(out[1], base[1], atol=2e-6, rtol=1e-5)
-        # one variant everywhere: every bucket runs it
+        # one variant everywhere: every bucket runs it, all in one launch (stack of
+        # t0 = 0 + search + re-pick)
         plan.set_variant(0)
         assert all(b[3] == 0 for b in plan.buckets())
         plan.run()
+        assert plan.stats()["kernel_launches"] == 3
         out0 = plan.download()
         assert np.mean(out0[0] == base[0]) >= 0.995
 
