@@ -114,7 +114,7 @@ __device__ void de_eval(const DeParams& R, int64_t e0, int64_t e1, float Tsec, c
 #pragma unroll
     for (int j = 0; j < W; ++j) acsq = __fadd_rn(acsq, __fmul_rn(num[q][j], num[q][j]));
     const float mf = (float)M[q];
-    const bool ok = ((double)den[q] > 1e-13) && ((double)mf > 1e-13) && (err[q] < 2);
+    const bool ok = (den[q] > kEpsilonF) && (M[q] > 0) && (err[q] < 2);
     sem[q] = ok ? __fdiv_rn(acsq, __fmul_rn(den[q], mf)) : 0.f;
     stk[q] = ok ? __fdiv_rn(lin[q], __fmul_rn((float)W, mf)) : 0.f;
   }

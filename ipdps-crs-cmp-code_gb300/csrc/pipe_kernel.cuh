@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
       const float den = kahan_hi[r * NT + threadIdx.x] - kahan_lo[r * NT + threadIdx.x];
       const float mf = (float)fa[r].M;
       const int err = tg.napert - fa[r].M;
-      const bool ok = ((double)den > 1e-13) && (fa[r].M > 0) && (err < 2);
+      const bool ok = (den > kEpsilonF) && (fa[r].M > 0) && (err < 2);
       const float sem = ok ? __fdividef(acsq, den * mf) : kSent;
       const float stk = ok ? __fdividef(lin, (float)W * mf) : kSent;
       const int idx = __float_as_int(__ldg(&cand[r].w));   // -1: padding slot

@@ -280,7 +280,7 @@ static __global__ void k_crs_stt00(int ncdps, KParams P, float a, float b, float
   }
   const int err = (int)(e1 - e0) - M;
   const float mf = (float)M;
-  const bool ok = ((double)den > 1e-13) && ((double)mf > 1e-13) && err < 2;
+  const bool ok = (den > kEpsilonF) && (mf > kEpsilonF) && err < 2;
   out[cdp] = ok ? __fdiv_rn(lin, __fmul_rn((float)W, mf)) : 0.0f;
 }
 

@@ -1003,7 +1003,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
           for (int j = 0; j < W; ++j) acsq = __fadd_rn(acsq, __fmul_rn(pa[r].num[j], pa[r].num[j]));
           const float mf = (float)pa[r].M;
           const int err = napert - pa[r].M;
-          const bool ok = ((double)pa[r].den > 1e-13) && ((double)mf > 1e-13) && (err < 2);
+          const bool ok = (pa[r].den > kEpsilonF) && (mf > kEpsilonF) && (err < 2);
           sem = ok ? __fdiv_rn(acsq, __fmul_rn(pa[r].den, mf)) : kSent;
           stk = ok ? __fdiv_rn(pa[r].lin, __fmul_rn((float)W, mf)) : kSent;
         } else {
@@ -1012,7 +1012,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
           const float den = kahan_hi[r * NT + threadIdx.x] - kahan_lo[r * NT + threadIdx.x];
           const float mf = (float)fa[r].M;
           const int err = napert - fa[r].M;
-          const bool ok = ((double)den > 1e-13) && (fa[r].M > 0) && (err < 2);
+          const bool ok = (den > kEpsilonF) && (fa[r].M > 0) && (err < 2);
           sem = ok ? __fdividef(acsq, den * mf) : kSent;
           stk = ok ? __fdividef(lin, (float)W * mf) : kSent;
         }
