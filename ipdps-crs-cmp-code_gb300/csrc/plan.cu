@@ -837,8 +837,9 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   SEMB_CUDA(cudaMemcpyAsync(pl->d_tasks, tasks.data(), tasks.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
 
   // aperture buckets (batched form): contiguous ranges of the sorted queue split at
-  // kBucketAp traces, each searched by its own launch with its own variant; a
-  // bucket too small to fill the GPU a few times over joins its larger neighbour
+  // kBucketAp traces, each with its own variant (neighbours on the same variant
+  // share a launch); a bucket too small to fill the GPU a few times over joins its
+  // larger neighbour
   {
     auto ap_of = [&](size_t t) { return (int)(ap_off[tasks[t].x + 1] - ap_off[tasks[t].x]); };
     std::vector<Bucket> bs;
@@ -913,7 +914,6 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   SEMB_CUDA(cudaStreamSynchronize(st));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, pl->ev[4], pl->ev[5]);
-
 
   std::memset(&pl->stats, 0, sizeof(pl->stats));
   pl->stats.ms_upload = ms;
@@ -1188,7 +1188,10 @@ int semb_plan_run(semb_plan* pl) {
       SEMB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       int rc = enqueue_run(pl, false);
       cudaError_t e = cudaStreamEndCapture(st, &graph);
-      if (rc != SEMB_OK) return rc;
+      if (rc != SEMB_OK) {
+        if (e == cudaSuccess) cudaGraphDestroy(graph);
+        return rc;
+      }
       SEMB_CUDA(e);
       e = cudaGraphInstantiate(&pl->graph, graph, 0);
       cudaGraphDestroy(graph);
@@ -1270,6 +1273,8 @@ int semb_plan_neighbours(semb_plan* pl, int32_t* off, int32_t* list, int64_t* n_
   if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_neighbours before semb_plan_upload");
   SEMB_CUDA(cudaSetDevice(pl->device));
   if (n_out) *n_out = pl->n_nbr;
+  if (off && pl->n_nbr > INT32_MAX)
+    return fail(SEMB_E_ARG, "%lld neighbour pairs do not fit 32-bit offsets", (long long)pl->n_nbr);
   if (off) {
     std::vector<int64_t> o(pl->ncdps + 1);
     SEMB_CUDA(cudaMemcpy(o.data(), pl->d_nbr_off, o.size() * 8, cudaMemcpyDeviceToHost));

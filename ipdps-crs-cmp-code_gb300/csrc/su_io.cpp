@@ -19,6 +19,7 @@
 // builds), traces of different ns are rejected.
 #include <algorithm>
 #include <cerrno>
+#include <cstdarg>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
