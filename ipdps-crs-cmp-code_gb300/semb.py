@@ -37,10 +37,12 @@ OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODE
 
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
-    "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_stream", "semb_plan_run", "semb_plan_download",
-    "semb_plan_download_attrs", "semb_survey_write_attr", "semb_plan_download_abc", "semb_survey_write_abc",
-    "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats", "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy", "semb_host_alloc",
-    "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count", "semb_strerror", "semb_last_error", "semb_abi_version",
+    "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_stream", "semb_plan_run",
+    "semb_plan_download", "semb_plan_download_attrs", "semb_survey_write_attr", "semb_plan_download_abc",
+    "semb_survey_write_abc", "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats",
+    "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy",
+    "semb_host_alloc", "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count",
+    "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
 
 
