@@ -2,6 +2,7 @@
 the host cores) and the DRAM-traffic figures it takes from the ncu summaries."""
 import json
 import os
+import socket
 import subprocess
 import sys
 
@@ -49,3 +50,21 @@ def test_traffic_from_profiles_scales_by_trace_evaluations():
     assert bench.traffic_from_profiles("no-such-workload", 1, 1) is None
     smem = bench.smem_from_profiles("crs-uneven-20k")
     assert 0 < smem["load_wavefronts_pct_of_peak"] <= 100 and smem["source"].startswith("ncu")
+
+
+def test_reference_arm_under_torchrun_prints_from_rank_0_only():
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_build")):
+        pytest.skip("oracle not built (build() compiles it)")
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
+                        "--gpus", "2", "--impl", "reference", "--workload", "cmp-4096-uneven", "--ncdp", "48",
+                        "--steps", "1", "--warmup", "3", "--cpu-sample", "4"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
