@@ -1,6 +1,6 @@
 """Generate the golden fixtures in this directory (run where the reference tree is).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]     (default: every case)
 
 Writes small seeded SU inputs and the outputs of the reference's own OpenMP
 programs on them, built from the reference sources by oracle/Makefile (make ref):
@@ -56,13 +56,18 @@ def cases():
     out.append(("crs_uneven_w5", synth.crs_survey(seed=105, ncdp=14, ns=200, dt_us=4000, na=2, nb=3, nc=4,
                                                   tau=0.008, aph=500, apm=60, azimuth=90.0,
                                                   aperture_range=(6, 40), block=4, line_len=7)))
+    # CMP at the largest window the reference allows (tau = 7 samples, w = 15 < MAX_W = 16)
+    out.append(("cmp_wmax", synth.cmp_survey(seed=106, ncmp=8, fold=12, ns=300, dt_us=4000, nc=12, tau=0.028)))
     return out
 
 
 def main():
     if not oracle.have_reference():
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    only = set(sys.argv[1:])
     for name, s in cases():
+        if only and name not in only:
+            continue
         d = os.path.join(HERE, name)
         shutil.rmtree(d, ignore_errors=True)
         os.makedirs(d)
