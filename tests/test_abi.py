@@ -62,3 +62,24 @@ def test_plan_argument_checks_need_no_device(semb_lib):
         with pytest.raises(semb.SembError) as e:
             semb.Plan(semb.params(semb.CMP, **kw))
         assert e.value.code == semb.E_ARG
+
+
+def test_extension_parameters_are_checked_before_the_device(semb_lib):
+    crs = dict(a0=-1e-3, a1=1e-3, na=2, b0=-1e-7, b1=1e-7, nb=2, c0=1e-7, c1=2e-7, nc=2, aph=100, apm=25,
+               tau=0.002)
+    bad = [
+        (semb.CRS, dict(dm_mode=7), crs),                                  # unknown displacement mode
+        (semb.CRS, dict(attrs=2), crs),                                    # attrs is 0 or 1
+        (semb.CRS, dict(ngen=-1), crs),                                    # negative generations
+        (semb.CRS, dict(ngen=3, mode=semb.BATCHED), crs),                  # CRS-DE is plain-form only
+        (semb.CMP, dict(ngen=3), dict(c0=1e-7, c1=2e-7, nc=4, aph=100, tau=0.002)),   # CRS only
+        (semb.CRS, dict(ngen=3), dict(crs, na=7, nb=7, nc=7)),             # population 343 > 256
+        (semb.CRS, dict(storage=5), crs),                                  # unknown storage
+        (semb.CRS, dict(repick=3), crs),                                   # unknown re-pick mode
+        (semb.CRS, {}, dict(crs, azimuth=float("nan"))),                   # azimuth must be finite
+        (semb.CRS, {}, dict(crs, na=0)),                                   # empty grid axis
+    ]
+    for method, opts, kw in bad:
+        with pytest.raises(semb.SembError) as e:
+            semb.Plan(semb.params(method, **opts, **kw))
+        assert e.value.code == semb.E_ARG, (opts, kw)
