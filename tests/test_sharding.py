@@ -1,4 +1,4 @@
-"""Multi-process sharding (CPU, gloo, world size 2).
+"""Multi-process sharding (CPU, gloo, world sizes 2 and 3).
 
 Each rank owns a contiguous CDP range and loads, read-only, the halo CDPs within
 apm; the CRS search of its owned CDPs must then equal the single-process search.
@@ -68,10 +68,29 @@ def test_split_ranges_balance_and_cover():
         assert all(a[1] == b[0] for a, b in zip(r, r[1:]))
 
 
-def test_two_ranks_reproduce_single_process_search(tmp_path):
+def test_halo_holds_every_neighbour_of_the_owned_cdps():
+    s = _survey()
+    g = oracle.gather(s.headers, s.samples, "crs", s.params["aph"], s.params["apm"], real=np.float32)
+    first = np.concatenate([[0], g["ntraces_by_cdp_id"][:-1]])
+    first_hdr = {k: g[k][first] for k in ("gx", "gy", "sx", "sy", "scalco")}
+    cdp_end = g["ntraces_by_cdp_id"].astype(np.int64)
+    mx, my = shard.first_trace_midpoints(first_hdr)
+    for world in (1, 2, 3, 5):
+        owned_all = []
+        for rank in range(world):
+            sh = shard.plan_shard("crs", cdp_end, first_hdr, s.params["apm"], world, rank)
+            lo, hi = sh.owned
+            owned_all.extend(range(lo, hi))
+            assert np.array_equal(sh.cdps[sh.owned_local], np.arange(lo, hi))
+            for nb in shard.neighbours_of(mx, my, s.params["apm"], range(lo, hi)):
+                assert np.isin(nb, sh.cdps).all()
+        assert owned_all == list(range(len(cdp_end)))
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_ranks_reproduce_single_process_search(tmp_path, world):
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
-    world = 2
     path = str(tmp_path / "gathered.npy")
     mp.start_processes(_worker, args=(world, _free_port(), path), nprocs=world, join=True, start_method="spawn")
     gathered = np.load(path, allow_pickle=True)
