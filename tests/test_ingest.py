@@ -135,3 +135,27 @@ def test_attribute_writer(case, semb_lib):
         hc, _ = su.read_su(os.path.join(d, f"{method}.coher.su"))
     assert np.array_equal(sx, data)
     assert hx.tobytes() == hc.tobytes()
+
+
+def test_explicit_parameter_writer_matches_the_grid_writer(semb_lib):
+    """semb_survey_write_abc (CRS-DE outputs) writes the same five files, with the same
+    headers, as the grid-search writer; the samples are the given A, B, C (C back in the
+    reference's unscaled units is the caller's), coherence and stack."""
+    meta, h, s, path = G.load("crs_line")
+    p = meta["params"]
+    sv = semb.Survey.load(path, semb.CRS, p["aph"])
+    a = sv.arrays()
+    ncdp, ns = len(a["cdp"]), a["ns"]
+    rng = np.random.default_rng(3)
+    vals = [rng.standard_normal((ncdp, ns)).astype(np.float32) for _ in range(5)]
+    ctr = np.zeros((ncdp, ns), np.int32)
+    with tempfile.TemporaryDirectory() as d1, tempfile.TemporaryDirectory() as d2:
+        sv.write(semb.params(semb.CRS, **p), ctr, vals[3], vals[4], d1)
+        sv.write_abc(*vals, d2)
+        for k, name in enumerate(("a", "b", "c", "coher", "stack")):
+            h1, _ = su.read_su(os.path.join(d1, f"crs.{name}.su"))
+            h2, x2 = su.read_su(os.path.join(d2, f"crs.{name}.su"))
+            assert h1.tobytes() == h2.tobytes(), name
+            assert np.array_equal(x2, vals[k]), name
+    with pytest.raises(semb.SembError):
+        semb.Survey.load(G.load("cmp_line")[3], semb.CMP, 800).write_abc(*vals, ".")
