@@ -240,20 +240,24 @@ int semb_plan_neighbours(semb_plan* plan, int32_t* off, int32_t* list, int64_t* 
 
 /* Neighbour lists with no device allocation.  No counterpart in the reference.
  *
- * For callers that cannot call cudaMalloc while they run (device memory owned by
- * another allocator, allocation-free real-time loops, work recorded into a CUDA
- * graph).  The caller passes device pointers: the first trace's gx, gy, sx, sy
- * and scalco of each of ncdps CDPs (inputs) and off[ncdps+1] and list[capacity]
- * (outputs, the same lists semb_plan_neighbours returns for a plan).  Scratch
- * lives in one fixed array inside this library, 2.5 MB on every GPU that loads
- * it, kept until the process exits, so ncdps is limited to 131072 (larger is
+ * For callers that cannot call cudaMalloc while they run: a pipeline whose device
+ * memory belongs to another allocator (a framework's caching pool, buffers
+ * registered with a communication library), or a real-time loop that forbids
+ * allocation after start-up.  The caller passes device pointers: the first trace's
+ * gx, gy, sx, sy and scalco of each of ncdps CDPs (inputs) and off[ncdps+1] and
+ * list[capacity] (outputs, the same lists semb_plan_neighbours returns for a plan).
+ * Scratch lives in one fixed array inside this library, 2.5 MB on every GPU that
+ * loads it, kept until the process exits, so ncdps is limited to 131072 (larger is
  * SEMB_E_ARG).  The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress), so make one call before any stream capture.  The call
- * enqueues on `stream` (a cudaStream_t, NULL for the legacy default stream) and
- * synchronizes it to return the list length in *n_list; if that exceeds
- * capacity the lists are truncated and SEMB_E_ARG is returned.  All calls share
- * the scratch: calls that overlap on the GPU (other threads, other streams)
- * race and must be serialized by the caller. */
+ * (cudaGetSymbolAddress) with the device current and keeps it for later calls, so
+ * make that first call before any stream capture; a cudaDeviceReset voids the kept
+ * address, and the entry point must not be used after one.  The call enqueues on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) and synchronizes it
+ * to return the list length in *n_list; if that exceeds capacity the lists are
+ * truncated and SEMB_E_ARG is returned (with *n_list set).  The search is all
+ * pairs, 2 x ncdps^2 distance tests (count, then fill): about 3.4e10 at the limit.
+ * All calls share the scratch: calls that overlap on the GPU (other threads, other
+ * streams) race and must be serialized by the caller. */
 int semb_neighbours_noalloc(const int32_t* gx, const int32_t* gy, const int32_t* sx, const int32_t* sy,
                             const int32_t* scalco, int32_t ncdps, int32_t apm, int32_t* off, int32_t* list,
                             int64_t capacity, int64_t* n_list, void* stream);

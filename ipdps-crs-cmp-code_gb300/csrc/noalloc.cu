@@ -2,16 +2,18 @@
 //
 // For callers that cannot allocate device memory while they run: a pipeline whose
 // device memory is owned by another allocator (a framework pool, a
-// pre-registered communication buffer), a real-time loop that forbids allocation
-// after start-up, or code being recorded into a CUDA graph, where cudaMalloc is
-// not allowed.  They pass their own device buffers for inputs and outputs; the
-// intermediate per-CDP midpoints, counts and offsets live in one file-scope
-// __device__ array of fixed size that every GPU loading this library holds until
-// the process exits.
+// pre-registered communication buffer), or a real-time loop that forbids
+// allocation after start-up.  They pass their own device buffers for inputs and
+// outputs; the intermediate per-CDP midpoints, counts and offsets live in one
+// file-scope __device__ array of fixed size that every GPU loading this library
+// holds until the process exits.  The array's device address is looked up once
+// per device (the first call on that device, with it current) and kept; a
+// cudaDeviceReset voids it.
 //
 // The search plan builds the same lists (semb_plan_upload), with scratch it
 // allocates itself; the arithmetic here is the same: CDP j is a neighbour of CDP i
-// when the float distance of their first-trace midpoints is within apm.
+// when the float distance of their first-trace midpoints is within apm.  The
+// search is all pairs (a count pass and a fill pass over ncdps^2 pairs).
 #include <cuda_runtime.h>
 
 #include <climits>

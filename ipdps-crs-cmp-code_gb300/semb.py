@@ -402,15 +402,18 @@ class PinnedArray:
 
 
 def neighbours_noalloc(gx_ptr, gy_ptr, sx_ptr, sy_ptr, scalco_ptr, ncdps: int, apm: int, off_ptr, list_ptr,
-                       capacity: int, stream_ptr=None) -> int:
+                       capacity: int, stream_ptr=None, check: bool = True):
     """semb_neighbours_noalloc on caller-owned device buffers (raw device pointers
-    as ints).  Returns the list length."""
-    n = C.c_int64()
-    _check(lib().semb_neighbours_noalloc(C.c_void_p(gx_ptr), C.c_void_p(gy_ptr), C.c_void_p(sx_ptr),
-                                         C.c_void_p(sy_ptr), C.c_void_p(scalco_ptr), int(ncdps), int(apm),
-                                         C.c_void_p(off_ptr), C.c_void_p(list_ptr), int(capacity), C.byref(n),
-                                         C.c_void_p(stream_ptr) if stream_ptr else None),
-           "semb_neighbours_noalloc")
+    as ints).  Returns the list length; with check=False returns (status, length)
+    instead of raising on a non-zero status."""
+    n = C.c_int64(-1)
+    rc = lib().semb_neighbours_noalloc(C.c_void_p(gx_ptr), C.c_void_p(gy_ptr), C.c_void_p(sx_ptr),
+                                       C.c_void_p(sy_ptr), C.c_void_p(scalco_ptr), int(ncdps), int(apm),
+                                       C.c_void_p(off_ptr), C.c_void_p(list_ptr), int(capacity), C.byref(n),
+                                       C.c_void_p(stream_ptr) if stream_ptr else None)
+    if not check:
+        return int(rc), int(n.value)
+    _check(rc, "semb_neighbours_noalloc")
     return int(n.value)
 
 
