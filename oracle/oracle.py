@@ -56,6 +56,8 @@ def lib():
         _lib.semb_oracle_max_threads.restype = i32
         _lib.semb_oracle_set_threads.argtypes = [i32]
         _lib.semb_oracle_set_dm.argtypes = [i32, f64]
+        _lib.semb_oracle_set_t0.argtypes = [i32, i32]
+        _lib.semb_oracle_set_top2.argtypes = [P]
         for sfx in ("_f32", "_f64"):
             f = getattr(_lib, "semb_oracle_crs_de" + sfx)
             f.restype = i32
@@ -144,9 +146,27 @@ def _list(cdps):
     return a, len(a)
 
 
+def _sampling(L, ncdp, ns, t0_range, top2):
+    """Set the t0 range and the top-2 gap output of the next search; returns the
+    gap array (NaN where not evaluated) or None."""
+    lo, hi = t0_range if t0_range is not None else (0, 0)
+    L.semb_oracle_set_t0(int(lo), int(hi))
+    gap = np.full(ncdp * ns, np.nan) if top2 else None
+    L.semb_oracle_set_top2(_p(gap))
+    return gap
+
+
+def _unset(L):
+    L.semb_oracle_set_t0(0, 0)
+    L.semb_oracle_set_top2(None)
+
+
 def cmp(g: dict, params: dict, precision: str = "f32", sem_all: bool = False, threads: int = 0,
-        cdps=None) -> dict:
-    """CMP search of the gather (all CDPs, or only the CDP indices in `cdps`)."""
+        cdps=None, t0_range=None, top2: bool = False) -> dict:
+    """CMP search of the gather (all CDPs, or only the CDP indices in `cdps`).
+    t0_range=(lo, hi) evaluates only those output samples (other rows stay zero);
+    top2=True adds out["top2"], the gap between the best and second-best candidate
+    semblance per (CDP, t0)."""
     L = lib()
     if threads:
         L.semb_oracle_set_threads(threads)
@@ -161,21 +181,27 @@ def cmp(g: dict, params: dict, precision: str = "f32", sem_all: bool = False, th
     secs = np.zeros(1, np.float64)
     lst, nlst = _list(cdps)
     fn = getattr(L, "semb_oracle_cmp_" + precision)
-    rc = fn(ncdp, _p(g["ntraces_by_cdp_id"]), ns, g["dt_us"], _p(g["samples"]),
-            _p(g["gx"]), _p(g["gy"]), _p(g["sx"]), _p(g["sy"]), _p(g["scalco"]),
-            parsed("cmp", params["c0"]), parsed("cmp", params["c1"]), nc, parsed("cmp", params["tau"]),
-            _p(ctr), _p(strr), _p(stk), _p(outc), _p(sem), _p(secs), _p(lst), nlst)
+    gap = _sampling(L, ncdp, ns, t0_range, top2)
+    try:
+        rc = fn(ncdp, _p(g["ntraces_by_cdp_id"]), ns, g["dt_us"], _p(g["samples"]),
+                _p(g["gx"]), _p(g["gy"]), _p(g["sx"]), _p(g["sy"]), _p(g["scalco"]),
+                parsed("cmp", params["c0"]), parsed("cmp", params["c1"]), nc, parsed("cmp", params["tau"]),
+                _p(ctr), _p(strr), _p(stk), _p(outc), _p(sem), _p(secs), _p(lst), nlst)
+    finally:
+        _unset(L)
     if rc != 0:
         raise RuntimeError(f"oracle cmp failed: {rc}")
     out = dict(ctr=ctr.reshape(ncdp, ns), str=strr.reshape(ncdp, ns), stk=stk.reshape(ncdp, ns),
                c=outc.reshape(ncdp, ns), seconds=float(secs[0]))
     if sem_all:
         out["sem_all"] = sem.reshape(ncdp, ns, nc)
+    if top2:
+        out["top2"] = gap.reshape(ncdp, ns)
     return out
 
 
 def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, threads: int = 0,
-        cdps=None, dm_signed: bool = False) -> dict:
+        cdps=None, dm_signed: bool = False, t0_range=None, top2: bool = False) -> dict:
     """CRS search of the gather (all CDPs, or only the CDP indices in `cdps`, with
     the neighbour lists of the whole gather).  `dm_signed` switches the midpoint
     displacement to the signed projection on params["azimuth"] (the library's
@@ -198,11 +224,15 @@ def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, th
     P = lambda k: parsed("crs", params[k])
     lst, nlst = _list(cdps)
     fn = getattr(L, "semb_oracle_crs_" + precision)
-    rc = fn(ncdp, _p(g["ntraces_by_cdp_id"]), ns, g["dt_us"], _p(g["samples"]),
-            _p(g["gx"]), _p(g["gy"]), _p(g["sx"]), _p(g["sy"]), _p(g["scalco"]),
-            _p(g["nbr_off"]), _p(g["nbr"]),
-            P("a0"), P("a1"), na, P("b0"), P("b1"), nb, P("c0"), P("c1"), nc, P("tau"),
-            _p(ctr), _p(strr), _p(stk), _p(oa), _p(ob), _p(oc), _p(sem), _p(secs), _p(nsem), _p(lst), nlst)
+    gap = _sampling(L, ncdp, ns, t0_range, top2)
+    try:
+        rc = fn(ncdp, _p(g["ntraces_by_cdp_id"]), ns, g["dt_us"], _p(g["samples"]),
+                _p(g["gx"]), _p(g["gy"]), _p(g["sx"]), _p(g["sy"]), _p(g["scalco"]),
+                _p(g["nbr_off"]), _p(g["nbr"]),
+                P("a0"), P("a1"), na, P("b0"), P("b1"), nb, P("c0"), P("c1"), nc, P("tau"),
+                _p(ctr), _p(strr), _p(stk), _p(oa), _p(ob), _p(oc), _p(sem), _p(secs), _p(nsem), _p(lst), nlst)
+    finally:
+        _unset(L)
     if rc != 0:
         raise RuntimeError(f"oracle crs failed: {rc}")
     out = dict(ctr=ctr.reshape(ncdp, ns), str=strr.reshape(ncdp, ns), stk=stk.reshape(ncdp, ns),
@@ -210,6 +240,8 @@ def crs(g: dict, params: dict, precision: str = "f64", sem_all: bool = False, th
                seconds=float(secs[0]), n_semblance_traces=int(nsem[0]))
     if sem_all:
         out["sem_all"] = sem.reshape(ncdp, ns, npar)
+    if top2:
+        out["top2"] = gap.reshape(ncdp, ns)
     return out
 
 

@@ -29,6 +29,14 @@
 static int semb_oracle_dm_signed = 0;
 static double semb_oracle_dm_cos = 1.0, semb_oracle_dm_sin = 0.0;
 
+/* Sampling of the checker (semb_oracle_set_t0, semb_oracle_set_top2): the searches
+ * evaluate only output samples t0 in [t0_lo, t0_hi) (the other rows are left as the
+ * caller initialised them), and, when top2 is set, write per (CDP, t0) the gap
+ * between the best and the second-best candidate semblance (double).  Neither
+ * changes the arithmetic of an evaluated item. */
+static int semb_oracle_t0_lo = 0, semb_oracle_t0_hi = 0x7fffffff;
+static double* semb_oracle_top2 = 0;
+
 #define REAL float
 #define SQRTR sqrtf
 #define SFX _f32
@@ -58,3 +66,14 @@ void semb_oracle_set_dm(int signed_dm, double azimuth_deg) {
   semb_oracle_dm_cos = cos(az);
   semb_oracle_dm_sin = sin(az);
 }
+
+/* Evaluate only t0 in [lo, hi) in the next searches (hi <= lo: every t0). */
+void semb_oracle_set_t0(int lo, int hi) {
+  if (hi <= lo) { lo = 0; hi = 0x7fffffff; }
+  semb_oracle_t0_lo = lo < 0 ? 0 : lo;
+  semb_oracle_t0_hi = hi;
+}
+
+/* Per (CDP, t0) gap best - second best of the next searches into out[ncdps * ns]
+ * (NULL: off). */
+void semb_oracle_set_top2(double* out) { semb_oracle_top2 = out; }

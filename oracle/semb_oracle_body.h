@@ -35,6 +35,18 @@ static inline int CAT(trunc_int, SFX)(REAL t, int* bad) {
   return (int)t;
 }
 
+/* Gap between the largest and the second-largest of n semblances (checker output,
+ * not part of the reference's computation). */
+static inline double CAT(top2_gap, SFX)(const REAL* v, int n) {
+  double b1 = -1e300, b2 = -1e300;
+  for (int i = 0; i < n; i++) {
+    const double x = (double)v[i];
+    if (x > b1) { b2 = b1; b1 = x; }
+    else if (x > b2) b2 = x;
+  }
+  return n > 1 ? b1 - b2 : 1e300;
+}
+
 /* CMP: CMP/OpenMP/src/main.cpp:88-241 (grid :119-122, half-offsets :125-136,
  * semblance :149-204, argmax :207-222, output values :253-255). */
 int CAT(semb_oracle_cmp, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int ns, int dt_us,
@@ -83,8 +95,10 @@ int CAT(semb_oracle_cmp, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
     const int t_idf = ntraces_by_cdp_id[cdp_id];
     const float* cdpsmpl = samples + (size_t)t_id0 * ns;
 
+    const int t0_lo = semb_oracle_t0_lo < ns ? semb_oracle_t0_lo : ns;
+    const int t0_hi = semb_oracle_t0_hi < ns ? semb_oracle_t0_hi : ns;
 #pragma omp parallel for schedule(static)
-    for (int i = 0; i < ns * nc; i++) {
+    for (int i = t0_lo * nc; i < t0_hi * nc; i++) {
       REAL _num[MAX_W_CMP], _ac_squared = 0, _ac_linear = 0, _den = 0, m = 0;
       int err = 0;
       int c_id = i % nc;
@@ -129,13 +143,14 @@ int CAT(semb_oracle_cmp, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
     if (sem_all) memcpy(sem_all + (size_t)cdp_id * ns * nc, num, sizeof(REAL) * (size_t)ns * nc);
 
 #pragma omp parallel for
-    for (int t0 = 0; t0 < ns; t0++) {
+    for (int t0 = t0_lo; t0 < t0_hi; t0++) {
       REAL max_sem = 0.0f;
       int max_c = -1;
       for (int it = t0 * nc; it < (t0 + 1) * nc; it++) {
         if (num[it] > max_sem) { max_sem = num[it]; max_c = it; }
       }
       size_t o = (size_t)cdp_id * ns + t0;
+      if (semb_oracle_top2) semb_oracle_top2[o] = CAT(top2_gap, SFX)(num + (size_t)t0 * nc, nc);
       ctr[o] = max_c % nc;
       str[o] = max_sem;
       stk[o] = max_c > -1 ? stt[max_c] : 0.0f;
@@ -264,9 +279,16 @@ int CAT(semb_oracle_crs, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
     }
     nsem += size;
 
+    const int t0_lo = semb_oracle_t0_lo < ns ? semb_oracle_t0_lo : ns;
+    const int t0_hi = semb_oracle_t0_hi < ns ? semb_oracle_t0_hi : ns;
+    /* a t0 range that skips t0 = 0 still evaluates that row: its candidate 0 gives
+     * the stack of the t0 without a pick (stt[max_par] with max_par = 0 below) */
+    const int extra = (t0_lo > 0 && t0_lo < t0_hi) ? 1 : 0;
+    const int nrows = (t0_hi > t0_lo ? t0_hi - t0_lo : 0) + extra;
 #pragma omp parallel for collapse(2) schedule(static)
-    for (int t0 = 0; t0 < ns; t0++) {
+    for (int row = 0; row < nrows; row++) {
       for (int par_id = 0; par_id < npar; par_id++) {
+        const int t0 = extra ? (row == 0 ? 0 : t0_lo + row - 1) : t0_lo + row;
         REAL _num[MAX_W_CRS], _ac_squared = 0, _ac_linear = 0, _den = 0, mm = 0;
         int err = 0;
         int id = t0 * npar + par_id;
@@ -313,13 +335,14 @@ int CAT(semb_oracle_crs, SFX)(int ncdps, const int32_t* ntraces_by_cdp_id, int n
     if (sem_all) memcpy(sem_all + (size_t)cdp_id * ns * npar, num, sizeof(REAL) * (size_t)ns * npar);
 
 #pragma omp parallel for
-    for (int t0 = 0; t0 < ns; t0++) {
+    for (int t0 = t0_lo; t0 < t0_hi; t0++) {
       REAL max_sem = 0.0f;
       int max_par = 0;
       for (int it = t0 * npar; it < (t0 + 1) * npar; it++) {
         if (num[it] > max_sem) { max_sem = num[it]; max_par = it; }
       }
       size_t o = (size_t)cdp_id * ns + t0;
+      if (semb_oracle_top2) semb_oracle_top2[o] = CAT(top2_gap, SFX)(num + (size_t)t0 * npar, npar);
       ctr[o] = max_par % npar;
       str[o] = max_sem;
       stk[o] = stt[max_par];

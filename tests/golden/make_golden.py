@@ -58,6 +58,14 @@ def cases():
                                                   aperture_range=(6, 40), block=4, line_len=7)))
     # CMP at the largest window the reference allows (tau = 7 samples, w = 15 < MAX_W = 16)
     out.append(("cmp_wmax", synth.cmp_survey(seed=106, ncmp=8, fold=12, ns=300, dt_us=4000, nc=12, tau=0.028)))
+    # tiny gathers: CMPs of two or three traces (w = 5 at 2 ms, 64 velocities), where
+    # near-tied velocities are resolved by few samples
+    out.append(("cmp_tiny", synth.cmp_survey(seed=107, ncmp=24, ns=500, dt_us=2000, nc=64, tau=0.004,
+                                             fold_range=(2, 3), hmax=1500.0, aph=1500)))
+    # CRS apertures of two traces of one CDP (CDPs farther apart than apm): dm = 0, so
+    # A and B do not change the traveltime and candidates tie exactly
+    out.append(("crs_tiny", synth.crs_survey(seed=108, ncdp=12, noffsets=2, ns=300, dt_us=4000, na=3, nb=3, nc=8,
+                                             tau=0.004, spacing=200.0, apm=50, aph=600)))
     return out
 
 

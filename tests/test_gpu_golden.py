@@ -4,8 +4,10 @@ the command lines.
 Plain form: semblance and stack within 1e-5 relative of the reference's
 single-precision build, and identical picks wherever the best two semblances
 (from the oracle's full table) differ by more than 1e-6.  Batched form: semblance
-within 1e-3 absolute of the reference's double-precision build and at least 99%
-identical picks."""
+within 1e-3 absolute of the reference's double-precision build, at least 99.5%
+identical picks, and 99.9% where the FP64 best two differ by more than 1e-6.
+The command lines (plain form) match the reference build of their own precision
+(FP32) and stay within a stated bound of the shipped CRS build (FP64)."""
 import os
 import subprocess
 
@@ -68,9 +70,13 @@ def test_batched_close_to_reference_f64(case):
     rows = G.rows_by_cdp(cdps, ref["coher"][0])
     assert np.max(np.abs(sem[rows] - ref["coher"][1])) <= 1e-3
     g = oracle.gather(h, s, method, meta["params"]["aph"], meta["params"].get("apm"), real=np.float64)
-    o = (oracle.cmp if method == "cmp" else oracle.crs)(g, meta["params"], "f64")
+    o = (oracle.cmp if method == "cmp" else oracle.crs)(g, meta["params"], "f64", top2=True)
     orow = G.rows_by_cdp(g["cdp_ids"], ref["coher"][0])
-    assert np.mean(ctr[rows] == o["ctr"][orow]) >= 0.99
+    same = ctr[rows] == o["ctr"][orow]
+    decisive = o["top2"][orow] > 1e-6
+    assert same.mean() >= 0.995, same.mean()
+    if decisive.any():
+        assert same[decisive].mean() >= 0.999, same[decisive].mean()
 
 
 @pytest.mark.parametrize("case", G.CASES)
@@ -84,20 +90,24 @@ def test_cli_end_to_end(case, tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "Execution Time" in r.stdout
     import su
-    prec = G.SHIPPED[method]
     mine = {a: su.read_su(str(tmp_path / f"{method}.{a}.su")) for a in G.ATTRS[method]}
-    ref = {a: su.read_su(G.ref_file(case, method, prec, a)) for a in G.ATTRS[method]}
+    shipped = {a: su.read_su(G.ref_file(case, method, G.SHIPPED[method], a)) for a in G.ATTRS[method]}
     for attr in G.ATTRS[method]:
-        assert np.array_equal(mine[attr][0].view(np.uint8), ref[attr][0].view(np.uint8)), attr
-    # the plain search is FP32; CMP ships FP32 (tight), CRS ships FP64, where a
-    # near tie may pick another candidate: compare the stack where picks agree
-    same = np.ones(mine["coher"][1].shape, bool)
+        assert np.array_equal(mine[attr][0].view(np.uint8), shipped[attr][0].view(np.uint8)), attr
+    # the command line searches in the plain form (FP32 arithmetic): against the
+    # reference's FP32 build the files match within 1e-5 relative, with the same
+    # picks where the best two differ by more than 1e-6
+    ref32 = {a: su.read_su(G.ref_file(case, method, "f32", a)) for a in G.ATTRS[method]}
+    np.testing.assert_allclose(mine["coher"][1], ref32["coher"][1], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(mine["stack"][1], ref32["stack"][1], rtol=1e-5, atol=1e-6)
+    gcdps, gap = _top2_gap(meta, h, s)
+    decisive = gap[G.rows_by_cdp(gcdps, ref32["coher"][0])] > 1e-6
     for a in G.ATTRS[method][:-2]:
-        same &= mine[a][1] == ref[a][1]
-    assert same.mean() >= 0.99
-    tol = 2e-6 if method == "cmp" else 2e-5
-    np.testing.assert_allclose(mine["coher"][1], ref["coher"][1], rtol=2e-5, atol=tol)
-    np.testing.assert_allclose(mine["stack"][1][same], ref["stack"][1][same], rtol=2e-5, atol=tol)
+        assert np.array_equal(mine[a][1][decisive], ref32[a][1][decisive]), a
+    # against the shipped CRS build (FP64): FP32 arithmetic stays within 1e-4 of the
+    # FP64 coherence (the reference's own FP32 build is within 8.5e-5 of its FP64 build
+    # on every golden case)
+    np.testing.assert_allclose(mine["coher"][1], shipped["coher"][1], rtol=0, atol=1e-4)
 
 
 @pytest.mark.parametrize("case", ["cmp_line", "crs_line"])

@@ -53,7 +53,7 @@ def test_crs_batched_close_to_oracle_f64(storage):
     (ctr, sem, stk), st = _run(semb.CRS, g, s.params, mode=semb.BATCHED, storage=storage)
     tol = 5e-3 if storage == semb.STORE_BF16 else 1e-3
     assert np.max(np.abs(sem - ref["str"])) < tol
-    assert np.mean(ctr == ref["ctr"]) > 0.99
+    assert np.mean(ctr == ref["ctr"]) >= 0.995
 
 
 def test_cmp_batched_close_to_oracle_f64():
@@ -62,7 +62,7 @@ def test_cmp_batched_close_to_oracle_f64():
     ref = oracle.cmp(g, s.params, "f64")
     (ctr, sem, stk), st = _run(semb.CMP, g, s.params, mode=semb.BATCHED)
     assert np.max(np.abs(sem - ref["str"])) < 1e-3
-    assert np.mean(ctr == ref["ctr"]) > 0.99
+    assert np.mean(ctr == ref["ctr"]) >= 0.995
 
 
 def test_crs_neighbour_lists_match_reference_rule():
@@ -107,7 +107,7 @@ def test_crs_signed_dm_batched_close_to_oracle_f64():
     ref = oracle.crs(g, p, "f64", dm_signed=True)
     (ctr, sem, stk), _ = _run(semb.CRS, g, p, mode=semb.BATCHED, dm_mode=semb.DM_SIGNED)
     assert np.max(np.abs(sem - ref["str"])) < 1e-3
-    assert np.mean(ctr == ref["ctr"]) > 0.99
+    assert np.mean(ctr == ref["ctr"]) >= 0.995
     # and it is not the |dm| result
     absr = oracle.crs(g, p, "f64")
     assert not np.allclose(absr["str"], ref["str"])
