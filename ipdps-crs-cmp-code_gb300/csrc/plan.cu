@@ -1081,6 +1081,7 @@ int enqueue_repick(semb_plan* pl, cudaStream_t st) {
     R.tau = pl->tau;
     R.method = p.method;
     R.mode = p.repick;
+    R.ncand = pl->ncand;
     R.dt = pl->dt64;
     R.idt = pl->idt64;
     R.gap = p.repick_gap;

@@ -315,6 +315,7 @@ struct RepickParams {
   const double* cand64;        // grid order: (a, b, c) x ncand, c in 1e6-scaled units
   const float* stt00;
   int ncdps, ns, tau, method, mode;
+  int ncand;                   // candidates of the grid (full re-search of small items)
   double dt, idt;
   float gap;
   int32_t* ctr;
@@ -327,10 +328,86 @@ struct RepickParams {
   float* err64;    // |FP32 - FP64 semblance| of the pick where re-evaluated, else -1
 };
 
+// Near-tie threshold of an item with `napert` aperture traces: the FP16 store's
+// rounding moves a semblance by about 2^-11 / sqrt(napert * w) of its value (random
+// rounding errors average over the traces and window samples), so small gathers
+// need a wider band than `gap`, which is sized for ~64 traces and up.
+__device__ __forceinline__ float repick_band(float gap, int napert) {
+  return gap * fmaxf(1.0f, sqrtf(64.0f / (float)max(napert, 1)));
+}
+
+// Items with at most this many (aperture trace x candidate) pairs are re-searched
+// over every candidate in FP64 when their FP32 top-4 lie within the near-tie band
+// (then a candidate outside the top-4 may be the FP64 best).
+constexpr int64_t kFullResearch = 16384;
+
+// Semblance and stack of candidate c at sample t0 in FP64 with the reference's
+// double-precision arithmetic, operation by operation and trace by trace in
+// aperture order (CMP/OpenMP/src/main.cpp:149-204, CRS/OpenMP/src/main.cpp:209-267
+// with real = double): every multiply and add rounded on its own.  Returns false
+// when the item is invalid (the reference's -1 / 0).
+template <int W>
+__device__ bool eval_f64_ordered(const RepickParams& R, int64_t e0, int64_t e1, int t0, int c, double& sem,
+                                 double& stk) {
+  const double pa = R.cand64[3 * (int64_t)c], pb = R.cand64[3 * (int64_t)c + 1], pc = R.cand64[3 * (int64_t)c + 2];
+  double num[W], den = 0.0, lin = 0.0, mm = 0.0;
+  int err = 0;
+#pragma unroll
+  for (int j = 0; j < W; ++j) num[j] = 0.0;
+  double T = __dmul_rn(R.dt, (double)t0);
+  if (R.method == METHOD_CMP) T = __dmul_rn(T, T);
+  for (int64_t e = e0; e < e1; ++e) {
+    const Geo64 g = R.ap_geo64[e];
+    double t;
+    if (R.method == METHOD_CMP) {
+      t = __dmul_rn(__dsqrt_rn(__dadd_rn(T, __dmul_rn(pc, g.h))), R.idt);
+    } else {
+      t = __dadd_rn(T, __dmul_rn(pa, g.m));
+      t = __dadd_rn(__dadd_rn(__dmul_rn(t, t), __dmul_rn(pb, g.m2)), __dmul_rn(pc, g.h));
+      t = t < 0.0 ? -1.0 : __dsqrt_rn(t);
+      t = __dmul_rn(t, R.idt);
+    }
+    // (int)t as the reference; a traveltime outside the int range counts as out of range
+    const bool bad = !(t > -2147483648.0 && t < 2147483647.0);
+    const int it = bad ? 0 : (int)t;
+    const double x = __dsub_rn(t, (double)it);
+    if (!bad && it - R.tau >= 0 && it + R.tau + 1 < R.ns) {
+      const float* s = R.samples + (int64_t)R.ap_tr[e] * R.pitch + (it - R.tau);
+      double s1 = s[0];
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        const double s0 = s1;
+        s1 = s[j + 1];
+        const double v = __dadd_rn(__dmul_rn(__dsub_rn(s1, s0), x), s0);
+        num[j] = __dadd_rn(num[j], v);
+        den = __dadd_rn(den, __dmul_rn(v, v));
+        lin = __dadd_rn(lin, v);
+      }
+      mm = __dadd_rn(mm, 1.0);
+    } else {
+      ++err;
+    }
+  }
+  double acsq = 0.0;
+#pragma unroll
+  for (int j = 0; j < W; ++j) acsq = __dadd_rn(acsq, __dmul_rn(num[j], num[j]));
+  if (den > 1e-13 && mm > 1e-13 && err < 2) {
+    sem = __ddiv_rn(acsq, __dmul_rn(den, mm));
+    stk = __ddiv_rn(lin, __dmul_rn((double)W, mm));
+    return true;
+  }
+  sem = stk = 0.0;
+  return false;
+}
+
 // Final pick per (CDP, t0), one warp each.  When the best two FP32 candidates are
-// closer than `gap` (or always, in mode 2) the top-4 are re-evaluated in FP64 with
-// the reference's double-precision arithmetic (CRS/OpenMP/src/main.cpp:209-267 with
-// real = double) on the FP32 samples, and the pick follows the FP64 values.
+// closer than the near-tie band (repick_band: `gap`, wider for small apertures), or
+// always in mode 2, the top-4 are re-evaluated in FP64 with the reference's
+// double-precision arithmetic (CRS/OpenMP/src/main.cpp:209-267 with real = double)
+// on the FP32 samples, and the pick follows the FP64 values.  Small items whose
+// whole top-4 lies inside the band are re-searched over every candidate instead
+// (eval_f64_ordered, one candidate per lane), so that a candidate the FP32 ranking
+// put fifth or lower can still win as it does in FP64.
 template <int W>
 static __global__ void k_repick(RepickParams R) {
   const int lane = threadIdx.x & 31;
@@ -349,18 +426,57 @@ static __global__ void k_repick(RepickParams R) {
   int ti0[kTopK];   // the list before the candidates out of reach are dropped
 #pragma unroll
   for (int q = 0; q < kTopK; ++q) ti0[q] = ti[q];
+  const int64_t e0 = R.ap_off[cdp], e1 = R.ap_off[cdp + 1];
+  const int napert = (int)(e1 - e0);
+  const float band = repick_band(R.gap, napert);
   const bool none = !(ts[0] > 0.f) || ti[0] < 0;
-  const bool near_tie = ti[1] >= 0 && ts[1] > 0.f && (ts[0] - ts[1]) < R.gap;
+  const bool near_tie = ti[1] >= 0 && ts[1] > 0.f && (ts[0] - ts[1]) < band;
   const bool redo = !none && (R.mode == 2 || (R.mode == 1 && near_tie));
-  // candidates that can still win: the best and those within `gap` of it (all
+  // the whole top-4 inside the band: the FP64 best may be outside it
+  const bool full = redo && ti[kTopK - 1] >= 0 && (ts[0] - ts[kTopK - 1]) < band &&
+                    (int64_t)napert * R.ncand <= kFullResearch;
+  // candidates that can still win: the best and those within the band of it (all
   // four in mode 2); the others keep their single-precision rank below the best
 #pragma unroll
   for (int q = 1; q < kTopK; ++q)
-    if (ti[q] >= 0 && !(R.mode == 2 || (ts[0] - ts[q]) < R.gap)) ti[q] = -1;
+    if (ti[q] >= 0 && !(R.mode == 2 || (ts[0] - ts[q]) < band)) ti[q] = -1;
   int out_i = ti[0];
   float out_s = ts[0], out_k = tk[0];
   float err = -1.f;
-  if (redo) {
+  if (full) {
+    // every candidate, one per lane, in FP64 in the reference's order; the pick is
+    // the reference's: the largest semblance above 0, the lowest index on ties
+    double bs = 0.0, bk = 0.0;
+    int bi = 0x7fffffff;
+    for (int c = lane; c < R.ncand; c += 32) {
+      double sem, stk;
+      if (eval_f64_ordered<W>(R, e0, e1, t0, c, sem, stk) && sem > bs) {
+        bs = sem;
+        bi = c;
+        bk = stk;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double os = __shfl_xor_sync(0xffffffffu, bs, o);
+      const double ok = __shfl_xor_sync(0xffffffffu, bk, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (os > bs || (os == bs && oi < bi)) {
+        bs = os;
+        bi = oi;
+        bk = ok;
+      }
+    }
+    if (bi != 0x7fffffff) {
+      out_i = bi;
+      out_s = (float)bs;
+      out_k = (float)bk;
+#pragma unroll
+      for (int q = 0; q < kTopK; ++q)
+        if (ti0[q] == bi) err = (float)fabs((double)ts[q] - bs);
+    }
+    if (lane == 0) atomicAdd(R.repicked, 1ull);
+  } else if (redo) {
     double num[kTopK][W], den[kTopK], lin[kTopK];
     int M[kTopK];
 #pragma unroll
@@ -379,7 +495,6 @@ static __global__ void k_repick(RepickParams R) {
       pb[q] = R.cand64[3 * (int64_t)c + 1];
       pc[q] = R.cand64[3 * (int64_t)c + 2];
     }
-    const int64_t e0 = R.ap_off[cdp], e1 = R.ap_off[cdp + 1];
     const double T = R.dt * (double)t0;
     for (int64_t e = e0 + lane; e < e1; e += 32) {
       const Geo64 g = R.ap_geo64[e];
@@ -425,7 +540,6 @@ static __global__ void k_repick(RepickParams R) {
         M[q] += __shfl_xor_sync(0xffffffffu, M[q], o);
       }
     }
-    const int napert = (int)(e1 - e0);
     double bs = 0.0;
     int bi = 0x7fffffff;
     double bk = 0.0;

@@ -265,21 +265,40 @@ def crs_survey(seed=2, ncdp=500, noffsets=48, ns=1000, dt_us=2000, nevents=4, na
     return s
 
 
-def config(idx: int, ncdp: int | None = None, **kw) -> Survey:
-    """The five benchmark workloads (index 0-4), optionally with fewer CDPs."""
+def config(idx: int, ncdp: int | None = None, segment: int = 0, **kw) -> Survey:
+    """The five benchmark workloads (index 0-4), optionally with fewer CDPs.
+
+    segment > 0 gives another, independent stretch of the same survey: the same
+    shapes drawn from another seed (seed + 7919 * segment), its CDP numbers after
+    the previous segments' and its coordinates 100 km further along x, so that no
+    CDP of one segment lies within the midpoint aperture of another's.  A multi-GPU
+    run gives segment r to rank r (weak scaling: per-GPU work stays fixed)."""
+    if segment:
+        base = _config(idx, ncdp, seed_shift=7919 * segment, **kw)
+        n = base.info["ncdp"]
+        base.headers["cdp"] += n * segment
+        shift = np.int32(10_000_000 * segment)   # cm
+        for k in ("sx", "gx"):
+            base.headers[k] += shift
+        base.name += f"-segment{segment}"
+        return base
+    return _config(idx, ncdp, **kw)
+
+
+def _config(idx: int, ncdp: int | None = None, seed_shift: int = 0, **kw) -> Survey:
     if idx == 0:
-        return cmp_survey(seed=0, ncmp=ncdp or 200, name="cmp-200x60-ns1000-nc101", **kw)
+        return cmp_survey(seed=0 + seed_shift, ncmp=ncdp or 200, name="cmp-200x60-ns1000-nc101", **kw)
     if idx == 1:
-        return cmp_survey(seed=1, ncmp=ncdp or 4096, ns=2000, dt_us=2000, nevents=8, nc=256, tau=0.004,
+        return cmp_survey(seed=1 + seed_shift, ncmp=ncdp or 4096, ns=2000, dt_us=2000, nevents=8, nc=256, tau=0.004,
                           aph=3000, fold_range=(12, 240), hmax=3000.0, name="cmp-4096-fold12to240-ns2000-nc256", **kw)
     if idx == 2:
-        return crs_survey(seed=2, ncdp=ncdp or 500, name="crs-500x48-ns1000-21x21x21", **kw)
+        return crs_survey(seed=2 + seed_shift, ncdp=ncdp or 500, name="crs-500x48-ns1000-21x21x21", **kw)
     if idx == 3:
-        return crs_survey(seed=3, ncdp=ncdp or 20000, ns=1500, dt_us=4000, nevents=6, tau=0.004, aph=2600,
+        return crs_survey(seed=3 + seed_shift, ncdp=ncdp or 20000, ns=1500, dt_us=4000, nevents=6, tau=0.004, aph=2600,
                           apm=150, azimuth=90.0, aperture_range=(50, 2000), block=32,
                           name="crs-20k-ap50to2000-ns1500-21x21x21", **kw)
     if idx == 4:
-        return crs_survey(seed=4, ncdp=ncdp or 100000, ns=1500, dt_us=4000, nevents=6, na=31, nb=31, nc=31,
+        return crs_survey(seed=4 + seed_shift, ncdp=ncdp or 100000, ns=1500, dt_us=4000, nevents=6, na=31, nb=31, nc=31,
                           tau=0.004, aph=2600, apm=150, azimuth=90.0, aperture_range=(50, 2000), block=32,
                           name="crs-100k-ap50to2000-ns1500-31x31x31", **kw)
     raise ValueError(f"unknown workload {idx}")
