@@ -104,3 +104,22 @@ def test_ranks_reproduce_single_process_search(tmp_path, world):
         assert np.array_equal(stk.view(np.uint32), full["stk"][lo:hi].view(np.uint32))
         covered[lo:hi] = True
     assert covered.all()
+
+
+def test_bench_segments_are_independent_surveys():
+    """A multi-GPU bench run gives rank r segment r of the workload: the same
+    shapes from another seed, CDP numbers after the earlier segments' and
+    coordinates far enough apart that no CRS CDP has a neighbour in another
+    segment; segment 0 is the one-GPU workload itself."""
+    a = synth.config(3, ncdp=64)
+    b = synth.config(3, ncdp=64, segment=1)
+    assert np.array_equal(synth.config(3, ncdp=64, segment=0).samples, a.samples)
+    assert a.headers["cdp"].max() < b.headers["cdp"].min()
+    assert not np.array_equal(a.samples[:10], b.samples[:10])
+    fa = np.concatenate([[0], np.cumsum(a.info["fold"])[:-1]])
+    fb = np.concatenate([[0], np.cumsum(b.info["fold"])[:-1]])
+    both = {k: np.concatenate([a.headers[k][fa], b.headers[k][fb]]) for k in ("gx", "gy", "sx", "sy", "scalco")}
+    mx, my = shard.first_trace_midpoints(both)
+    lists = shard.neighbours_of(mx, my, a.params["apm"], range(len(mx)))
+    n = len(fa)
+    assert all(np.all(nb < n) for nb in lists[:n]) and all(np.all(nb >= n) for nb in lists[n:])
