@@ -509,7 +509,9 @@ def run_ours(args, rank, world, dist):
     gap = {} if args.repick_gap is None else {"repick_gap": args.repick_gap}
     plan = semb.Plan(semb.params(method, mode=semb.BATCHED, storage=storage, **gap, **s.params), device=dev)
     plan.upload(arrays.view())
-    tune = plan.autotune() if args.tune else None
+    if args.variant is not None:
+        plan.set_variant(args.variant)
+    tune = plan.autotune() if args.tune and args.variant is None else None
     buckets = plan.buckets()
     st0 = plan.stats()
     nap = int(round(st0["trace_evals"] / (st0["ns"] * st0["ncand"])))
@@ -686,6 +688,7 @@ def main():
                     help="near-tie threshold of the FP64 re-pick (default: the library's)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--variant", type=int, default=None, help="force this search-kernel variant (no autotuning)")
     ap.add_argument("--no-target", action="store_true", help="skip the 20k-CDP CRS goal leg")
     ap.add_argument("--target-ncdp", type=int, default=None, help="CDPs of the goal leg's survey (default 20000)")
     ap.add_argument("--target-err-per-bucket", type=int, default=8,

@@ -29,10 +29,10 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 7
+#define SEMB_ABI_VERSION 8
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
-#define SEMB_MAX_VARIANTS 16
+#define SEMB_MAX_VARIANTS 24
 
 /* Aperture buckets of a batched plan's work queue (semb_plan_buckets). */
 #define SEMB_MAX_BUCKETS 4
@@ -308,6 +308,28 @@ int semb_plan_buckets(const semb_plan* plan, int32_t* nbuckets, int32_t* ap_lo, 
 /* Use search-kernel variant `variant` (0..SEMB_MAX_VARIANTS-1) for later runs; SEMB_E_ARG when this
  * plan's window and form have no such variant.  No counterpart in the reference. */
 int semb_plan_set_variant(semb_plan* plan, int32_t variant);
+
+/* Batched form: stage at most max_samples window samples per chunk in shared memory
+ * (0, the default: as much as the kernel variant's resident CTAs per SM leave, at
+ * least 512).  A trace whose window is larger than the stage is read from the FP32
+ * store in global memory instead; results are those of the staged path (bit for bit
+ * with SEMB_STORE_F32).  Smaller stages let more CTAs share an SM.  Takes effect at
+ * once on an uploaded plan.  No counterpart in the reference. */
+int semb_plan_set_staging(semb_plan* plan, int32_t max_samples);
+
+/* Batched grid search in chunks of cdps_per_chunk contiguous CDPs (0, the default:
+ * the whole survey at once).  semb_plan_run then searches the chunks one after the
+ * other; each chunk's work (the CRS t0 = 0 stacks, one search launch per run of
+ * aperture buckets on the same kernel variant, the FP64 re-pick of its samples) is
+ * captured as a CUDA graph on the chunk's first run and replayed on later runs.
+ * Results equal the unchunked run's.  No counterpart in the reference, which
+ * searches CDP by CDP (CRS/CUDA/src/main.cu:420-450). */
+int semb_plan_set_chunks(semb_plan* plan, int32_t cdps_per_chunk);
+
+/* Device time of each chunk of the last chunked run: *nchunks gets the number of
+ * chunks and ms[0..min(max, nchunks)-1] their milliseconds (0 chunks after an
+ * unchunked run). */
+int semb_plan_chunk_times(const semb_plan* plan, int32_t max, double* ms, int32_t* nchunks);
 
 /* Capture the search (work-queue reset + kernels) in a CUDA graph and replay it on
  * later semb_plan_run calls (batched form).  on = 0 goes back to direct launches. */

@@ -56,12 +56,13 @@ int launch_search(int method, int form, int w, int v, const KParams& P, int nwar
   return SEMB_OK;
 }
 
-int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st) {
-  const int grid = (ncdps + 127) / 128;
+int launch_stt00(int w, int cdp0, int cdp1, const KParams& P, float a, float b, float c, float* out, cudaStream_t st) {
+  const int grid = (cdp1 - cdp0 + 127) / 128;
+  if (grid <= 0) return SEMB_OK;
   switch (w) {
-    case 1: k_crs_stt00<1><<<grid, 128, 0, st>>>(ncdps, P, a, b, c, out); break;
-    case 3: k_crs_stt00<3><<<grid, 128, 0, st>>>(ncdps, P, a, b, c, out); break;
-    case 5: k_crs_stt00<5><<<grid, 128, 0, st>>>(ncdps, P, a, b, c, out); break;
+    case 1: k_crs_stt00<1><<<grid, 128, 0, st>>>(cdp0, cdp1, P, a, b, c, out); break;
+    case 3: k_crs_stt00<3><<<grid, 128, 0, st>>>(cdp0, cdp1, P, a, b, c, out); break;
+    case 5: k_crs_stt00<5><<<grid, 128, 0, st>>>(cdp0, cdp1, P, a, b, c, out); break;
     default: return fail(SEMB_E_WINDOW, "no CRS kernel for w = %d", w);
   }
   SEMB_CUDA(cudaGetLastError());
@@ -69,7 +70,8 @@ int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, 
 }
 
 int launch_repick(int w, const RepickParams& R, cudaStream_t st) {
-  const int64_t items = (int64_t)R.ncdps * R.ns;
+  const int64_t items = R.item_end - R.item0;
+  if (items <= 0) return SEMB_OK;
   const int grid = (int)((items + 7) / 8);
   switch (w) {
     case 1: k_repick<1><<<grid, 256, 0, st>>>(R); break;

@@ -352,6 +352,11 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
           const float u0 = fmaf(CA(0), g.x, Tsmp);
           q0 = fmaf(u0, u0, CC(0) * g.z);
         }
+        if (soff == kGlobalEntry) {
+          // a window larger than a stage: the items read the FP32 store
+          global_entry<METHOD, BRUN>(P, meta->raw[e], g, q0, Tsmp, T2smp, span, ca2, cb2, cc2, fa);
+          continue;
+        }
 #pragma unroll
         for (int r = 0; r < RC; ++r) {
           float t2;

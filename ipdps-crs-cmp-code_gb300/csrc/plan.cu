@@ -43,7 +43,9 @@ int grid_neighbours(int ncdps, const float* d_fmx, const float* d_fmy, int apm, 
                     int64_t* n_out, cudaStream_t st);
 // CDP count from which the CRS neighbour lists come from the grid search
 constexpr int kGridNeighbours = 2048;
-int launch_stt00(int w, int ncdps, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
+// smallest automatic staging capacity of the batched form (samples per chunk)
+constexpr int kMinStage = 512;
+int launch_stt00(int w, int cdp0, int cdp1, const KParams& P, float a, float b, float c, float* out, cudaStream_t st);
 int launch_repick(int w, const RepickParams& R, cudaStream_t st);
 int launch_crs_de(int w, const DeParams& R, cudaStream_t st);
 
@@ -146,6 +148,21 @@ struct semb_plan {
   cudaEvent_t ev[6] = {};
   bool use_graph = false;
   cudaGraphExec_t graph = nullptr;
+  int stage_cap = 0;   // batched form: most staged samples per chunk (0: as shared memory allows)
+  // chunked runs (semb_plan_set_chunks): contiguous CDP chunks searched one after the
+  // other, each chunk's work (CRS t0 = 0 stacks, search launches per aperture bucket,
+  // FP64 re-pick) captured once as a CUDA graph and replayed on later runs
+  struct RunChunk {
+    int cdp0 = 0, cdp1 = 0;
+    std::vector<int> bucket_begin;   // [nbuckets + 1] task ranges in d_chunk_tasks
+    cudaGraphExec_t graph = nullptr;
+  };
+  int chunk_cdps = 0;
+  bool chunks_dirty = true;
+  std::vector<RunChunk> run_chunks;
+  int2* d_chunk_tasks = nullptr;
+  std::vector<cudaEvent_t> chunk_ev;
+  std::vector<double> chunk_ms;
   semb_stats stats{};
 };
 
@@ -190,6 +207,10 @@ void free_cfg(KernelCfg& c) {
 void drop_graph(semb_plan* pl) {
   if (pl->graph) cudaGraphExecDestroy(pl->graph);
   pl->graph = nullptr;
+  for (auto& c : pl->run_chunks)
+    if (c.graph) cudaGraphExecDestroy(c.graph);
+  pl->run_chunks.clear();
+  pl->chunks_dirty = true;
 }
 
 // Device buffer *p of n elements, kept from the previous upload when it is large
@@ -241,8 +262,8 @@ void free_data(semb_plan* pl, bool keep_reusable = false) {
   release(pl->d_de_a);
   release(pl->d_de_b);
   release(pl->d_de_c);
-  if (pl->graph) cudaGraphExecDestroy(pl->graph);
-  pl->graph = nullptr;
+  drop_graph(pl);
+  release(pl->d_chunk_tasks);
   pl->uploaded = false;
 }
 
@@ -380,14 +401,22 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
 
   // staging capacity, shared memory and residency, checked before the plan's
   // device state changes (a variant that does not fit leaves the plan as it was)
+  // The plain form stages whole windows always (capacity >= one trace).  The batched
+  // form reads a window larger than its staging capacity from the FP32 store in
+  // global memory (kGlobalEntry), so its stages need not hold a whole trace: the
+  // capacity is what the variant's resident CTAs per SM leave, at least kMinStage
+  // samples (or the plan's stage_cap, which also bounds it from above).
   const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
   const size_t budget = (227 * 1024) / minb - 1024;
   int cap = form == FORM_PLAIN ? 32768 : 8192;
+  if (form == FORM_FAST && pl->stage_cap > 0) cap = std::min(cap, pl->stage_cap);
   auto smem_of = [&](int cp) {
     return pipe ? pipe_layout(rc, cp, store, nt, lay).total : smem_layout(form, rc, cp, store, nt).total;
   };
   while (cap > 64 && smem_of(cap) > budget) cap -= 64;
-  if (cap < (int)pl->pitch + 16) cap = ((int)pl->pitch + 16 + 63) & ~63;
+  int min_cap = (int)pl->pitch + 16;
+  if (form == FORM_FAST) min_cap = std::min(min_cap, pl->stage_cap > 0 ? pl->stage_cap : kMinStage);
+  if (cap < min_cap) cap = (min_cap + 63) & ~63;
   const size_t smem = smem_of(cap);
   if (smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", pl->ns);
   int occ = 0;
@@ -555,6 +584,7 @@ int semb_plan_destroy(semb_plan* pl) {
     if (ev) cudaEventDestroy(ev);
   if (pl->copy_stream) cudaStreamSynchronize(pl->copy_stream);
   for (cudaEvent_t e : pl->chunk_done) cudaEventDestroy(e);
+  for (cudaEvent_t e : pl->chunk_ev) cudaEventDestroy(e);
   dev_free(pl->d_chunk_counter);
   if (pl->copy_done) cudaEventDestroy(pl->copy_done);
   if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
@@ -566,7 +596,7 @@ int semb_plan_destroy(semb_plan* pl) {
 namespace {
 int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks);
 int enqueue_streamed(semb_plan* pl, const semb_gather_view* g);
-int enqueue_repick(semb_plan* pl, cudaStream_t st);
+int enqueue_repick(semb_plan* pl, cudaStream_t st, int cdp0, int cdp1, bool reset_count);
 }  // namespace
 
 int semb_plan_upload(semb_plan* pl, const semb_gather_view* g) { return upload_impl(pl, g, 0); }
@@ -992,7 +1022,7 @@ int enqueue_run(semb_plan* pl, bool timed) {
     return SEMB_OK;
   }
   if (p.method == SEMB_CRS) {
-    SEMB_TRY(launch_stt00(pl->w, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
+    SEMB_TRY(launch_stt00(pl->w, 0, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
     ++launches;
   }
   if (p.ngen > 0) {
@@ -1053,7 +1083,7 @@ int enqueue_run(semb_plan* pl, bool timed) {
   }
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[2], st));
   if (form == FORM_FAST) {
-    SEMB_TRY(enqueue_repick(pl, st));
+    SEMB_TRY(enqueue_repick(pl, st, 0, pl->ncdps, true));
     ++launches;
   }
   if (timed) SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
@@ -1061,8 +1091,9 @@ int enqueue_run(semb_plan* pl, bool timed) {
   return SEMB_OK;
 }
 
-// The FP64 near-tie re-pick of the batched form, on stream st.
-int enqueue_repick(semb_plan* pl, cudaStream_t st) {
+// The FP64 near-tie re-pick of the batched form over CDPs [cdp0, cdp1) (every CDP
+// by default), on stream st; reset_count clears the re-picked-items counter first.
+int enqueue_repick(semb_plan* pl, cudaStream_t st, int cdp0, int cdp1, bool reset_count) {
   const semb_params& p = pl->p;
   {
     RepickParams R{};
@@ -1092,7 +1123,9 @@ int enqueue_repick(semb_plan* pl, cudaStream_t st) {
     R.sem2 = pl->d_sem2;
     R.idx2 = pl->d_idx2;
     R.err64 = pl->d_err64;
-    SEMB_CUDA(cudaMemsetAsync(pl->d_repicked, 0, sizeof(unsigned long long), st));
+    R.item0 = (int64_t)cdp0 * pl->ns;
+    R.item_end = (int64_t)cdp1 * pl->ns;
+    if (reset_count) SEMB_CUDA(cudaMemsetAsync(pl->d_repicked, 0, sizeof(unsigned long long), st));
     SEMB_TRY(launch_repick(pl->w, R, st));
   }
   return SEMB_OK;
@@ -1140,10 +1173,10 @@ int enqueue_streamed(semb_plan* pl, const semb_gather_view* g) {
   SEMB_CUDA(cudaStreamWaitEvent(st, pl->chunk_done[nk - 1], 0));
   if (p.method == SEMB_CRS) {
     const KParams P = make_kparams(pl, 0);
-    SEMB_TRY(launch_stt00(pl->w, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
+    SEMB_TRY(launch_stt00(pl->w, 0, pl->ncdps, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
     ++launches;
   }
-  SEMB_TRY(enqueue_repick(pl, st));
+  SEMB_TRY(enqueue_repick(pl, st, 0, pl->ncdps, true));
   ++launches;
   SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
   SEMB_CUDA(cudaStreamSynchronize(st));
@@ -1163,9 +1196,168 @@ int enqueue_streamed(semb_plan* pl, const semb_gather_view* g) {
   return SEMB_OK;
 }
 
+// Kernels one chunk launches (the same count its graph holds).
+int count_chunk_launches(const semb_plan* pl, const semb_plan::RunChunk& ch, int* n) {
+  *n = (pl->p.method == SEMB_CRS ? 1 : 0) + 1;
+  const int nb = (int)pl->buckets.size();
+  for (int i = 0; i < nb;) {
+    int j = i + 1;
+    while (j < nb && pl->buckets[j].cfg.variant == pl->buckets[i].cfg.variant) ++j;
+    if (ch.bucket_begin[j] > ch.bucket_begin[i]) ++*n;
+    i = j;
+  }
+  return SEMB_OK;
+}
+
+// The tasks of every run chunk (semb_plan_set_chunks): per chunk its CDPs by
+// decreasing aperture, split at the plan's aperture buckets so that each bucket's
+// tasks run with that bucket's kernel variant.
+int build_run_chunks(semb_plan* pl) {
+  drop_graph(pl);
+  dev_free(pl->d_chunk_tasks);
+  const int nb = (int)pl->buckets.size();
+  const int nblk = (pl->ns + kTB - 1) / kTB;
+  auto bucket_of = [&](int ap) {
+    for (int b = 0; b < nb; ++b)
+      if (ap >= pl->buckets[b].ap_lo) return b;
+    return nb - 1;
+  };
+  std::vector<int2> tasks;
+  tasks.reserve((size_t)pl->ncdps * nblk);
+  for (int c0 = 0; c0 < pl->ncdps; c0 += pl->chunk_cdps) {
+    semb_plan::RunChunk ch;
+    ch.cdp0 = c0;
+    ch.cdp1 = std::min(pl->ncdps, c0 + pl->chunk_cdps);
+    std::vector<int> cdps(ch.cdp1 - ch.cdp0);
+    std::iota(cdps.begin(), cdps.end(), ch.cdp0);
+    std::stable_sort(cdps.begin(), cdps.end(), [&](int x, int y) { return pl->aperture[x] > pl->aperture[y]; });
+    ch.bucket_begin.assign(nb + 1, 0);
+    size_t q = 0;
+    for (int b = 0; b < nb; ++b) {
+      ch.bucket_begin[b] = (int)tasks.size();
+      while (q < cdps.size() && bucket_of(pl->aperture[cdps[q]]) == b) {
+        for (int k = 0; k < nblk; ++k) tasks.push_back(make_int2(cdps[q], k * kTB));
+        ++q;
+      }
+    }
+    ch.bucket_begin[nb] = (int)tasks.size();
+    if (q != cdps.size()) return fail(SEMB_E_STATE, "aperture buckets do not cover chunk %d", (int)pl->run_chunks.size());
+    pl->run_chunks.push_back(std::move(ch));
+  }
+  SEMB_TRY(dev_alloc(&pl->d_chunk_tasks, tasks.size()));
+  SEMB_CUDA(cudaMemcpy(pl->d_chunk_tasks, tasks.data(), tasks.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  const size_t nev = pl->run_chunks.size() + 1;
+  while (pl->chunk_ev.size() < nev) {
+    cudaEvent_t e;
+    SEMB_CUDA(cudaEventCreate(&e));
+    pl->chunk_ev.push_back(e);
+  }
+  pl->chunks_dirty = false;
+  return SEMB_OK;
+}
+
+// One chunk's work on the plan's stream: CRS t0 = 0 stacks of its CDPs, the search
+// of its tasks (one launch per run of buckets on the same variant), the re-pick of
+// its (CDP, t0) items.
+int enqueue_chunk(semb_plan* pl, const semb_plan::RunChunk& ch, int* launches) {
+  cudaStream_t st = pl->stream;
+  const semb_params& p = pl->p;
+  SEMB_CUDA(cudaMemsetAsync(pl->d_counter, 0, kMaxBuckets * sizeof(int), st));
+  if (p.method == SEMB_CRS) {
+    const KParams P = make_kparams(pl, 0);
+    SEMB_TRY(launch_stt00(pl->w, ch.cdp0, ch.cdp1, P, pl->cand0_a, pl->cand0_b, pl->cand0_c, pl->d_stt00, st));
+    ++*launches;
+  }
+  const int nb = (int)pl->buckets.size();
+  for (int i = 0; i < nb;) {
+    int j = i + 1;
+    while (j < nb && pl->buckets[j].cfg.variant == pl->buckets[i].cfg.variant) ++j;
+    const int t0 = ch.bucket_begin[i], n = ch.bucket_begin[j] - t0;
+    if (n > 0) {
+      const KernelCfg& cfg = pl->buckets[i].cfg;
+      const KParams P = make_kparams_cfg(pl, cfg, pl->d_chunk_tasks + t0, n, pl->d_counter + i);
+      SEMB_TRY(launch_search(p.method, FORM_FAST, pl->w, cfg.variant, P, cfg.nwarps, std::min(n, pl->sms * cfg.occ),
+                             cfg.smem, st));
+      ++*launches;
+    }
+    i = j;
+  }
+  SEMB_TRY(enqueue_repick(pl, st, ch.cdp0, ch.cdp1, false));
+  ++*launches;
+  return SEMB_OK;
+}
+
+// A whole search in chunks (semb_plan_run with chunks set): each chunk's graph,
+// captured on its first run, replayed in order; per-chunk device times kept.
+int run_chunked(semb_plan* pl) {
+  cudaStream_t st = pl->stream;
+  if (pl->chunks_dirty) SEMB_TRY(build_run_chunks(pl));
+  SEMB_CUDA(cudaMemsetAsync(pl->d_repicked, 0, sizeof(unsigned long long), st));
+  int launches = 0;
+  const int nk = (int)pl->run_chunks.size();
+  SEMB_CUDA(cudaEventRecord(pl->ev[0], st));
+  SEMB_CUDA(cudaEventRecord(pl->chunk_ev[0], st));
+  for (int k = 0; k < nk; ++k) {
+    semb_plan::RunChunk& ch = pl->run_chunks[k];
+    int n = 0;
+    if (!ch.graph) {
+      cudaGraph_t graph;
+      SEMB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      const int rc = enqueue_chunk(pl, ch, &n);
+      const cudaError_t e = cudaStreamEndCapture(st, &graph);
+      if (rc != SEMB_OK) {
+        if (e == cudaSuccess) cudaGraphDestroy(graph);
+        return rc;
+      }
+      SEMB_CUDA(e);
+      const cudaError_t ei = cudaGraphInstantiate(&ch.graph, graph, 0);
+      cudaGraphDestroy(graph);
+      SEMB_CUDA(ei);
+    } else {
+      // the launch count of a replayed chunk: buckets on distinct variants with tasks
+      SEMB_TRY(count_chunk_launches(pl, ch, &n));
+    }
+    launches += n;
+    SEMB_CUDA(cudaGraphLaunch(ch.graph, st));
+    SEMB_CUDA(cudaEventRecord(pl->chunk_ev[k + 1], st));
+  }
+  SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
+  pl->stats.kernel_launches = launches;
+  return SEMB_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int semb_plan_set_chunks(semb_plan* pl, int32_t cdps_per_chunk) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (cdps_per_chunk < 0) return fail(SEMB_E_ARG, "cdps_per_chunk must be >= 0");
+  if (cdps_per_chunk > 0 && (pl->p.mode != SEMB_BATCHED || pl->p.ngen > 0))
+    return fail(SEMB_E_ARG, "chunked runs are the batched form's grid search");
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  pl->chunk_cdps = cdps_per_chunk;
+  drop_graph(pl);
+  return SEMB_OK;
+}
+
+int semb_plan_chunk_times(const semb_plan* pl, int32_t max, double* ms, int32_t* nchunks) {
+  if (!pl || !nchunks) return fail(SEMB_E_ARG, "null argument");
+  *nchunks = (int32_t)pl->chunk_ms.size();
+  for (int i = 0; ms && i < std::min<int>(max, (int)pl->chunk_ms.size()); ++i) ms[i] = pl->chunk_ms[i];
+  return SEMB_OK;
+}
+
+int semb_plan_set_staging(semb_plan* pl, int32_t max_samples) {
+  if (!pl) return fail(SEMB_E_ARG, "null argument");
+  if (max_samples != 0 && max_samples < 64) return fail(SEMB_E_ARG, "staging capacity %d below 64", max_samples);
+  pl->stage_cap = max_samples;
+  if (!pl->uploaded) return SEMB_OK;
+  SEMB_CUDA(cudaSetDevice(pl->device));
+  for (Bucket& b : pl->buckets) SEMB_TRY(build_cfg(pl, b.cfg.variant, b.cfg));
+  refresh_stats(pl);
+  return SEMB_OK;
+}
 
 int semb_plan_use_graph(semb_plan* pl, int32_t on) {
   if (!pl) return fail(SEMB_E_ARG, "null argument");
@@ -1183,7 +1375,12 @@ int semb_plan_run(semb_plan* pl) {
   SEMB_CUDA(cudaSetDevice(pl->device));
   cudaStream_t st = pl->stream;
   SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, sizeof(int), st));
-  if (pl->use_graph) {
+  const bool chunked = pl->chunk_cdps > 0 && pl->p.mode == SEMB_BATCHED && pl->p.ngen == 0 &&
+                       pl->ns >= 2 * pl->tau + 2;
+  pl->chunk_ms.clear();
+  if (chunked) {
+    SEMB_TRY(run_chunked(pl));
+  } else if (pl->use_graph) {
     if (!pl->graph) {
       cudaGraph_t graph;
       SEMB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1212,7 +1409,13 @@ int semb_plan_run(semb_plan* pl) {
     SEMB_CUDA(cudaMemcpy(&rep, pl->d_repicked, sizeof(rep), cudaMemcpyDeviceToHost));
   // graph replays are timed as a whole; the per-kernel split needs direct launches
   float a = 0.f, b = 0.f, c = 0.f;
-  if (!pl->use_graph) {
+  if (chunked) {
+    for (size_t k = 0; k < pl->run_chunks.size(); ++k) {
+      float m = 0.f;
+      SEMB_CUDA(cudaEventElapsedTime(&m, pl->chunk_ev[k], pl->chunk_ev[k + 1]));
+      pl->chunk_ms.push_back(m);
+    }
+  } else if (!pl->use_graph) {
     SEMB_CUDA(cudaEventElapsedTime(&a, pl->ev[1], pl->ev[2]));
     SEMB_CUDA(cudaEventElapsedTime(&b, pl->ev[2], pl->ev[3]));
   }

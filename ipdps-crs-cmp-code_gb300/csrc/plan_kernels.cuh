@@ -243,9 +243,9 @@ static __global__ void k_make_store16(int64_t ntr, int ns, int64_t pitch, int st
 // candidate has positive semblance (CRS/OpenMP/src/main.cpp:272-284, stt[max_par]
 // with max_par = 0).  One thread per CDP, traces summed in aperture order.
 template <int W>
-static __global__ void k_crs_stt00(int ncdps, KParams P, float a, float b, float c, float* __restrict__ out) {
-  const int cdp = blockIdx.x * blockDim.x + threadIdx.x;
-  if (cdp >= ncdps) return;
+static __global__ void k_crs_stt00(int cdp0, int cdp1, KParams P, float a, float b, float c, float* __restrict__ out) {
+  const int cdp = cdp0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (cdp >= cdp1) return;
   const int64_t e0 = P.ap_off[cdp], e1 = P.ap_off[cdp + 1];
   float num[W];
 #pragma unroll
@@ -316,6 +316,7 @@ struct RepickParams {
   const float* stt00;
   int ncdps, ns, tau, method, mode;
   int ncand;                   // candidates of the grid (full re-search of small items)
+  int64_t item0, item_end;     // (CDP, t0) items cdp * ns + t0 of this launch
   double dt, idt;
   float gap;
   int32_t* ctr;
@@ -411,8 +412,8 @@ __device__ bool eval_f64_ordered(const RepickParams& R, int64_t e0, int64_t e1, 
 template <int W>
 static __global__ void k_repick(RepickParams R) {
   const int lane = threadIdx.x & 31;
-  const int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (item >= (int64_t)R.ncdps * R.ns) return;
+  const int64_t item = R.item0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (item >= R.item_end) return;
   const int cdp = (int)(item / R.ns);
   const int t0 = (int)(item - (int64_t)cdp * R.ns);
   float ts[kTopK], tk[kTopK];

@@ -99,6 +99,11 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 13) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 512, 2>();
       if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 3, 7, 1, LAY_P2, true, 512>();
       if (variant == 15) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
+      // stages smaller than a trace (windows beyond them read from global memory):
+      // two 256-thread CTAs per SM, and 640 threads of 6 candidates
+      if (variant == 16) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 2, LAY_PD, METHOD == METHOD_CRS, 256, 2>();
+      if (variant == 17) return pipe_entry<METHOD, 3, 6, 1, LAY_PD, METHOD == METHOD_CRS, 640>();
+      if (variant == 18) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 2, LAY_P2, METHOD == METHOD_CRS, 256>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -116,6 +121,10 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 13) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_SD, METHOD == METHOD_CRS, 512>();
       if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 5, 7, 1, LAY_P2, true, 512>();
       if (variant == 15) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
+      // stages smaller than a trace: two 256-thread CTAs per SM
+      if (variant == 16) return pipe_entry<METHOD, 5, 7, 2, LAY_P2, METHOD == METHOD_CRS, 256>();
+      if (variant == 17) return pipe_entry<METHOD, 5, 6, 2, LAY_SD, METHOD == METHOD_CRS, 256>();
+      if (variant == 18) return pipe_entry<METHOD, 5, 7, 2, LAY_QUAD, METHOD == METHOD_CRS, 256>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;

@@ -63,6 +63,10 @@ constexpr int kMaxChunk = 128;   // aperture traces staged per chunk
 constexpr int kMargin = 2;       // extra samples on each side of a staged window
 constexpr int kTopK = 4;
 constexpr int kZeroSlots = 16;   // zero block after the staging buffer (floats or entries)
+// Entry offset (ChunkMeta::geo[].w) of a trace whose window does not fit the staging
+// buffer (batched form): its items read the FP32 store in global memory instead, and
+// ChunkMeta::raw holds its trace index.
+constexpr int kGlobalEntry = INT32_MIN;
 constexpr int kMaxThreads = 256; // CTA size limit of the search kernel (variants use 128 or 256)
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier wait (2 s), then error
 
@@ -186,7 +190,8 @@ struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
   float scale[kMaxChunk];  // fast form: per-trace scale of the 16-bit store
   int raw[kMaxChunk];      // fast form: start of the entry's raw window (samples):
-                           // its buffer offset + 8 x its rank in aperture order
+                           // its buffer offset + 8 x its rank in aperture order;
+                           // the trace index for a kGlobalEntry entry
   int n;                   // entries in this chunk
   int n_in;                // fast form: entries on which every item of the pass is in
                            // range, in slots [0, n_in); the others fill slots
@@ -317,6 +322,7 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
     bool inr = false, keep = false;
     int tr = 0;
     float sc = 1.0f;
+    bool glob = false;
     if (have) {
       g = P.ap_geo[k];
       keep = trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi, inr);
@@ -326,6 +332,12 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
         lo &= ~(ALIGN - 1);
         hi |= (ALIGN - 1);
         len = hi - lo + 1;
+        // batched form: a window larger than the whole buffer is not staged; its
+        // items read the FP32 store (the partly-in-range section checks each item)
+        if (FORM == FORM_FAST && len > P.cap) {
+          glob = true;
+          len = 0;
+        }
       }
     }
     // inclusive scan of the kept windows' lengths over the warp
@@ -340,7 +352,7 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
     const int stop = over ? __ffs(over) - 1 : 32;
     // the plain form keeps every entry in aperture order at the front
     const bool take = keep && lane < stop;
-    const bool front = FORM == FORM_PLAIN || inr;
+    const bool front = FORM == FORM_PLAIN || (inr && !glob);
     const unsigned fr = __ballot_sync(0xffffffffu, take && front);
     const unsigned bk = __ballot_sync(0xffffffffu, take && !front);
     if (take) {
@@ -348,11 +360,11 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
       const int e = front ? n_in + __popc(fr & below) : kMaxChunk - 1 - (n_out + __popc(bk & below));
       const int off = base + incl - len;
       const int rank = n_in + n_out + __popc((fr | bk) & below);   // in aperture order
-      g.w = __int_as_float(off - lo);
+      g.w = __int_as_float(glob ? kGlobalEntry : off - lo);
       meta->geo[e] = g;
       meta->scale[e] = sc;
-      meta->raw[e] = off + 8 * rank;
-      src[e] = make_int4(tr, lo, len, off);
+      meta->raw[e] = glob ? tr : off + 8 * rank;
+      src[e] = make_int4(tr, lo, len, off);   // len 0: nothing to copy or convert
     }
     const int nhave = __popc(__ballot_sync(0xffffffffu, have));
     base += stop > 0 ? __shfl_sync(0xffffffffu, incl, stop - 1) : 0;
@@ -550,6 +562,16 @@ struct FastAcc {
       }
     }
   }
+  // the same arithmetic on the window samples sv[0..W] of the FP32 store, for a
+  // trace whose window was not staged (the staged entries hold the same values)
+  __device__ __forceinline__ void add_samples(const float* sv, float x) {
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      const float v = fmaf(sv[j + 1] - sv[j], x, sv[j]);
+      num[j] += v;
+      den_c = fmaf(v, v, den_c);
+    }
+  }
   __device__ __forceinline__ float take_energy() {
     const float e = den_c;
     den_c = 0.f;
@@ -620,6 +642,29 @@ struct FastAcc<W, LAY_P2> {
       }
     }
   }
+  // add() on window samples sv[0..W] of the FP32 store (sv zero past W)
+  __device__ __forceinline__ void add_samples(const float* sv, float x) {
+    const float2 xx = make_float2(x, x);
+    float4 B = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; 4 * q < W; ++q) {
+      const int j0 = 4 * q;
+      if (j0 + 1 == W && q > 0) {
+        single(B.y, B.w, x);
+        break;
+      }
+      const float4 A = make_float4(sv[j0], sv[j0 + 2], sv[j0 + 1], sv[j0 + 3]);
+      if (j0 + 2 < W) pair(2 * q, make_float2(A.x, A.y), make_float2(A.z, A.w), xx);
+      if (j0 + 3 < W) {
+        B = make_float4(sv[j0 + 2], sv[j0 + 4], sv[j0 + 3], sv[j0 + 5]);
+        pair(2 * q + 1, make_float2(A.z, A.w), make_float2(B.x, B.y), xx);
+      } else if (j0 + 3 == W) {
+        single(A.z, A.y, x);
+      } else if (j0 + 1 == W) {
+        single(A.x, A.z, x);
+      }
+    }
+  }
   __device__ __forceinline__ float take_energy() {
     const float e = den2.x + den2.y;
     den2 = make_float2(0.f, 0.f);
@@ -655,8 +700,12 @@ struct FastAcc<W, LAY_PD> {
     den2 = make_float2(0.f, 0.f);
     M = 0;
   }
-  __device__ __forceinline__ void add(uint32_t a, float x) {
-    const float4 A = lds128(a);   // (s_0, s_2, d_0, d_2)
+  __device__ __forceinline__ void add(uint32_t a, float x) { acc(lds128(a), x); }
+  // add() on window samples sv[0..3] of the FP32 store
+  __device__ __forceinline__ void add_samples(const float* sv, float x) {
+    acc(make_float4(sv[0], sv[2], sv[1] - sv[0], sv[3] - sv[2]), x);
+  }
+  __device__ __forceinline__ void acc(const float4 A, float x) {   // A = (s_0, s_2, d_0, d_2)
     const float2 v = __ffma2_rn(make_float2(A.z, A.w), make_float2(x, x), make_float2(A.x, A.y));
     np = __fadd2_rn(np, v);
     den2 = __ffma2_rn(v, v, den2);
@@ -678,6 +727,41 @@ struct FastAcc<W, LAY_PD> {
 
 
 
+
+// Batched form: the items of one thread on a trace whose window was not staged
+// (kGlobalEntry): the traveltime as on the staged traces, then the window samples
+// from the FP32 store in global memory, checked against the record's ends.
+template <int METHOD, bool BRUN, int W, int LAY, int RC, int RP>
+__device__ __forceinline__ void global_entry(const KParams& P, int tr, float4 g, float q0, float Tsmp, float T2smp,
+                                             unsigned span, const float2 (&ca2)[RP], const float2 (&cb2)[RP],
+                                             const float2 (&cc2)[RP], FastAcc<W, LAY> (&fa)[RC]) {
+  const float* row = P.samples + (int64_t)tr * P.pitch;
+#pragma unroll
+  for (int r = 0; r < RC; ++r) {
+    const float ca = (r & 1) ? ca2[r >> 1].y : ca2[r >> 1].x;
+    const float cb = (r & 1) ? cb2[r >> 1].y : cb2[r >> 1].x;
+    const float cc = (r & 1) ? cc2[r >> 1].y : cc2[r >> 1].x;
+    float t2;
+    if (METHOD == METHOD_CMP) {
+      t2 = fmaf(cc, g.z, T2smp);
+    } else if (BRUN) {
+      t2 = fmaf(cb, g.y, q0);
+    } else {
+      const float u = fmaf(ca, g.x, Tsmp);
+      t2 = fmaf(u, u, fmaf(cb, g.y, cc * g.z));
+    }
+    const float t = sqrt_fast(t2);   // NaN for t2 < 0: out of range below
+    const float y = __fadd_rz(t, 8388608.0f);
+    const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
+    const bool ok = (unsigned)rel <= span;
+    const float x = ok ? t - (y - 8388608.0f) : 0.0f;
+    float sv[W + 8];
+#pragma unroll
+    for (int i = 0; i < W + 8; ++i) sv[i] = (ok && i <= W) ? __ldg(row + rel + i) : 0.f;
+    fa[r].add_samples(sv, x);
+    fa[r].M += ok ? 1 : 0;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // The search kernel.
@@ -898,6 +982,10 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
             if (BRUN && METHOD == METHOD_CRS) {
               const float u0 = fmaf(CA(0), g.x, Tsmp);
               q0 = fmaf(u0, u0, CC(0) * g.z);
+            }
+            if (soff == kGlobalEntry) {
+              global_entry<METHOD, BRUN>(P, meta->raw[e], g, q0, Tsmp, T2smp, span, ca2, cb2, cc2, fa);
+              continue;
             }
 #pragma unroll
             for (int r = 0; r < RC; ++r) {

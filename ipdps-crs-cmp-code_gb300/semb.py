@@ -29,8 +29,8 @@ PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
 DM_ABS, DM_SIGNED = 0, 1
-ABI_VERSION = 7
-MAX_VARIANTS = 16   # SEMB_MAX_VARIANTS
+ABI_VERSION = 8
+MAX_VARIANTS = 24   # SEMB_MAX_VARIANTS
 MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
 OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODEV = range(10)
@@ -40,7 +40,9 @@ EXPORTS = [
     "semb_survey_free", "semb_plan_create", "semb_plan_upload", "semb_plan_stream", "semb_plan_run",
     "semb_plan_download", "semb_plan_download_attrs", "semb_survey_write_attr", "semb_plan_download_abc",
     "semb_survey_write_abc", "semb_plan_neighbours", "semb_neighbours_noalloc", "semb_plan_stats",
-    "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_use_graph", "semb_plan_destroy",
+    "semb_plan_autotune", "semb_plan_buckets", "semb_plan_set_variant", "semb_plan_set_staging",
+    "semb_plan_set_chunks", "semb_plan_chunk_times",
+    "semb_plan_use_graph", "semb_plan_destroy",
     "semb_host_alloc", "semb_host_free", "semb_probe_fp32", "semb_selftest_wait", "semb_device_count",
     "semb_strerror", "semb_last_error", "semb_abi_version",
 ]
@@ -122,6 +124,9 @@ def lib():
         "semb_plan_autotune": (C.c_int, [P, P, P]),
         "semb_plan_buckets": (C.c_int, [P, P, P, P, P, P]),
         "semb_plan_set_variant": (C.c_int, [P, i32]),
+        "semb_plan_set_staging": (C.c_int, [P, i32]),
+        "semb_plan_set_chunks": (C.c_int, [P, i32]),
+        "semb_plan_chunk_times": (C.c_int, [P, i32, P, P]),
         "semb_plan_use_graph": (C.c_int, [P, i32]),
         "semb_plan_destroy": (C.c_int, [P]),
         "semb_host_alloc": (C.c_int, [C.c_size_t, P]),
@@ -358,6 +363,23 @@ class Plan:
 
     def set_variant(self, v: int) -> None:
         _check(lib().semb_plan_set_variant(self._h, int(v)), "semb_plan_set_variant")
+
+    def set_chunks(self, cdps_per_chunk: int) -> None:
+        """Run the batched grid search in chunks of contiguous CDPs, each chunk's
+        work one CUDA graph (0: the whole survey at once)."""
+        _check(lib().semb_plan_set_chunks(self._h, int(cdps_per_chunk)), "semb_plan_set_chunks")
+
+    def chunk_times(self) -> list:
+        """Device milliseconds of each chunk of the last chunked run."""
+        n = C.c_int32()
+        ms = (C.c_double * 4096)()
+        _check(lib().semb_plan_chunk_times(self._h, 4096, ms, C.byref(n)), "semb_plan_chunk_times")
+        return [float(ms[i]) for i in range(min(n.value, 4096))]
+
+    def set_staging(self, max_samples: int) -> None:
+        """Batched form: stage at most max_samples window samples per chunk (0:
+        automatic); larger windows are read from the FP32 store in global memory."""
+        _check(lib().semb_plan_set_staging(self._h, int(max_samples)), "semb_plan_set_staging")
 
     def stats(self) -> dict:
         s = SembStats()
