@@ -481,6 +481,97 @@ def run_target(args, dev):
     return out
 
 
+def run_chunked_survey(args):
+    """A whole survey in CDP chunks, each chunk's search + re-pick one CUDA graph
+    (semb_plan_set_chunks), one run; with the batched form's error against the FP64
+    oracle on a seeded sample of CDPs.  The oracle runs in a child process forked
+    before the first GPU call, on the host cores, while the GPU searches."""
+    t_gen = time.perf_counter()
+    s, method, cdp_end, _ = make_gather(args.workload, args.ncdp)
+    ncdp = len(cdp_end)
+    log(f"[chunked] generated {ncdp} CDPs, {s.ntraces} traces x {s.ns} samples in {time.perf_counter() - t_gen:.0f}s")
+    storage = {"f16": semb.STORE_F16, "bf16": semb.STORE_BF16, "f32": semb.STORE_F32}[args.storage]
+    rng = np.random.default_rng(args.err_seed)
+    n_err = max(1, int(round(ncdp * args.err_frac)))
+    idx = np.sort(rng.choice(ncdp, size=min(n_err, ncdp), replace=False))
+    nblk = (s.ns + 31) // 32
+    blocks = np.sort(rng.choice(nblk, size=min(args.err_t0_blocks, nblk), replace=False))
+    child, err_path = None, None
+    if not args.no_cpu:
+        err_path = tempfile.mktemp(prefix="semb_c4_oracle_", suffix=".npz")
+        child = os.fork()
+        if child == 0:   # CPU only: the FP64 oracle on the sample, then exit
+            try:
+                oracle = oracle_mod()
+                g, local = sub_gather(oracle, s, method, cdp_end, idx, "f64")
+                parts = {k: [] for k in ("ctr", "str", "stk", "top2")}
+                secs = 0.0
+                for b in blocks:
+                    lo, hi = 32 * int(b), min(s.ns, 32 * int(b) + 32)
+                    o = oracle_search(oracle, g, s, method, "f64", local, t0_range=(lo, hi), top2=True)
+                    secs += o["seconds"]
+                    for k in parts:
+                        parts[k].append(o[k][local, lo:hi])
+                np.savez(err_path, secs=secs, **{k: np.concatenate(v, axis=1) for k, v in parts.items()})
+                os._exit(0)
+            except BaseException as e:   # noqa: BLE001
+                print(f"[chunked] oracle child failed: {e!r}", file=sys.stderr, flush=True)
+                os._exit(1)
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    out = {"workload": args.workload, "name": s.name, "storage": args.storage, "ncdps": ncdp, "traces": s.ntraces,
+           "chunk_cdps": args.chunk_cdps}
+    with semb.Plan(semb.params(method, mode=semb.BATCHED, storage=storage, **s.params), device=dev) as plan:
+        t_up = time.perf_counter()
+        plan.upload(gather_arrays(s, cdp_end).view())
+        out["upload_s"] = time.perf_counter() - t_up
+        if args.tune:
+            t_tune = time.perf_counter()
+            v, ms = plan.autotune()
+            out["autotune"] = {"variant": v, "sample_ms": ms, "seconds": time.perf_counter() - t_tune,
+                               "buckets": [dict(zip(("ap_lo", "ap_hi", "tasks", "variant"), b))
+                                           for b in plan.buckets()]}
+        plan.set_chunks(args.chunk_cdps)
+        with ClockSampler(dev) as clk:
+            plan.run()
+        st = plan.stats()
+        chunk_ms = plan.chunk_times()
+        ap = plan.download_attrs(batched=False)["aperture"]
+        ctr, sem, stk = plan.download()
+    nap = int(ap.sum())
+    flops = algo_flops(method, st, nap)
+    peak = semb.probe_fp32_tflops(dev)
+    total_ms = st["ms_total"]
+    ach = flops / (total_ms * 1e-3) / 1e12
+    out.update(ncand=st["ncand"], window=st["window"], mean_aperture=float(ap.mean()), evals=st["evals"],
+               trace_evals=st["trace_evals"], ms_total=total_ms, chunks=len(chunk_ms), ms_per_chunk=chunk_ms,
+               evals_per_s=st["evals"] / (total_ms * 1e-3), repicked=st["repicked"],
+               kernel_launches=st["kernel_launches"], clocks=clk.summary(),
+               roofline={"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                         "note": "search + re-pick time of every chunk (graph replays give no split)",
+                         "peak_source": "measured live: semb_probe_fp32 FMA throughput"})
+    if child is not None:
+        _, status = os.waitpid(child, 0)
+        if status == 0 and os.path.exists(err_path):
+            ref = np.load(err_path)
+            t0s = np.concatenate([np.arange(32 * int(b), min(s.ns, 32 * int(b) + 32)) for b in blocks])
+            c, sm, sk = (a[np.ix_(idx, t0s)] for a in (ctr, sem, stk))
+            same = c == ref["ctr"]
+            decisive = ref["top2"] > 1e-6
+            out["error_vs_fp64"] = {
+                "sample": f"{len(idx)} seeded CDPs ({args.err_frac:.1%}) x {len(t0s)} t0 in {len(blocks)} blocks, "
+                          f"FP64 oracle ({float(ref['secs']):.0f} s on the host cores)",
+                "pairs": int(same.size), "decisive_pairs": int(decisive.sum()),
+                "sem_max_abs": float(np.max(np.abs(sm - ref["str"]))),
+                "stack_max_abs": float(np.max(np.abs(sk - ref["stk"]))),
+                "identical_picks": float(same.mean()),
+                "identical_picks_decisive": float(same[decisive].mean()) if decisive.any() else None}
+            os.unlink(err_path)
+        else:
+            out["error_vs_fp64"] = {"failed": f"oracle child exit status {status}"}
+    print(json.dumps({"chunked_survey": out}), flush=True)
+    return 0
+
+
 def run_ours(args, rank, world, dist):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     t_gen = time.perf_counter()
@@ -689,6 +780,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--variant", type=int, default=None, help="force this search-kernel variant (no autotuning)")
+    ap.add_argument("--chunk-cdps", type=int, default=0,
+                    help="instead of the benchmark line: one run of the whole workload in chunks of this many CDPs "
+                         "(one CUDA graph per chunk) with FP64 errors on a sample")
+    ap.add_argument("--err-frac", type=float, default=0.01, help="chunked run: fraction of CDPs in the error sample")
+    ap.add_argument("--err-t0-blocks", type=int, default=1, help="chunked run: 32-sample t0 blocks per sampled CDP")
+    ap.add_argument("--err-seed", type=int, default=17, help="chunked run: seed of the error sample")
     ap.add_argument("--no-target", action="store_true", help="skip the 20k-CDP CRS goal leg")
     ap.add_argument("--target-ncdp", type=int, default=None, help="CDPs of the goal leg's survey (default 20000)")
     ap.add_argument("--target-err-per-bucket", type=int, default=8,
@@ -715,6 +812,11 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference_arm(args, rank, world)
+        if args.chunk_cdps > 0:
+            if world > 1:
+                log("the chunked whole-survey run is a one-GPU run")
+                return 2
+            return run_chunked_survey(args)
         return run_ours(args, rank, world, dist)
     finally:
         if dist is not None:

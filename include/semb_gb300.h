@@ -18,6 +18,12 @@
  * belong to the caller.  A plan owns its device memory and one CUDA stream; plans
  * are not shared between threads.  Nothing here falls back to the CPU: without a
  * usable GPU, semb_plan_create fails with SEMB_E_NODEV.
+ *
+ * libsemb_gb300_checked.so exports the same ABI with bounds-checked search kernels:
+ * every item that reads a staged sample window is tested against the window the
+ * planner staged for its trace, and a violation makes semb_plan_run return
+ * SEMB_E_BOUNDS with the first offending CDP, t0 and trace in the message (the
+ * production library clamps such an address to the buffer instead).
  */
 #ifndef SEMB_GB300_H
 #define SEMB_GB300_H
@@ -68,7 +74,9 @@ enum {
   SEMB_E_CUDA = 6,      /* a CUDA call failed */
   SEMB_E_TIMEOUT = 7,   /* a bounded device-side wait gave up */
   SEMB_E_STATE = 8,     /* call out of order (e.g. run before upload) */
-  SEMB_E_NODEV = 9      /* no usable CUDA device */
+  SEMB_E_NODEV = 9,     /* no usable CUDA device */
+  SEMB_E_BOUNDS = 10    /* checked build only: an item's sample window left the
+                           window staged for its trace (see libsemb_gb300_checked) */
 };
 
 /* Search parameters, with the meaning of the reference's command-line flags

@@ -31,6 +31,10 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp
 
 LIB_SOURCES = ["su_io.cpp", "plan.cu", "launch.cu", "search_cmp_plain.cu", "search_cmp_fast.cu",
                "search_crs_plain.cu", "search_crs_fast.cu", "probe.cu", "noalloc.cu", "neighbours.cu", "de.cu"]
+# the search kernels, compiled a second time with their window checks for the
+# checked library (libsemb_gb300_checked.so, the same ABI)
+SEARCH_SOURCES = ["search_cmp_plain.cu", "search_cmp_fast.cu", "search_crs_plain.cu", "search_crs_fast.cu"]
+CHECKED_LIB = os.path.join(OUT, "libsemb_gb300_checked.so")
 
 
 def nvcc() -> str:
@@ -59,17 +63,23 @@ def _compile(src: str, extra=()) -> str:
 
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    jobs = [(s, ()) for s in LIB_SOURCES] + [("cli.cpp", ("-DSEMB_CLI_METHOD=0",)),
-                                             ("cli.cpp", ("-DSEMB_CLI_METHOD=1",))]
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda j: _compile(*j), jobs))
-    lib_objs, cli_cmp, cli_crs = objs[:len(LIB_SOURCES)], objs[-2], objs[-1]
-    newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + lib_objs + ["-lcudart"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    jobs = [(s, ()) for s in LIB_SOURCES] + [(s, ("-DSEMB_CHECKED=1",)) for s in SEARCH_SOURCES] + [
+        ("cli.cpp", ("-DSEMB_CLI_METHOD=0",)), ("cli.cpp", ("-DSEMB_CLI_METHOD=1",))]
+    # the heaviest translation units (the search kernels) first
+    order = sorted(range(len(jobs)), key=lambda i: not jobs[i][0].startswith("search_"))
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        done = dict(zip(order, ex.map(lambda i: _compile(*jobs[i]), order)))
+    objs = [done[i] for i in range(len(jobs))]
+    nl, ns = len(LIB_SOURCES), len(SEARCH_SOURCES)
+    lib_objs, checked_objs, cli_cmp, cli_crs = objs[:nl], objs[nl:nl + ns], objs[-2], objs[-1]
+    checked_lib_objs = [o for o, src in zip(lib_objs, LIB_SOURCES) if src not in SEARCH_SOURCES] + checked_objs
+    for out, parts in ((LIB, lib_objs), (CHECKED_LIB, checked_lib_objs)):
+        newest = max(os.path.getmtime(o) for o in parts)
+        if not os.path.exists(out) or os.path.getmtime(out) < newest:
+            cmd = [nvcc()] + ARCH + ["-shared", "-o", out] + parts + ["-lcudart"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     for obj, name in ((cli_cmp, "cmp-gb300"), (cli_crs, "crs-gb300")):
         exe = os.path.join(OUT, name)
         if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(LIB), os.path.getmtime(obj)):

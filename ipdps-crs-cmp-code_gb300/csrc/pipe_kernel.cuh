@@ -338,6 +338,12 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
           const float2 t = make_float2(sqrt_fast(t2.x), sqrt_fast(t2.y));
           const float2 y = __fadd2_rz(t, kTwo23x2);
           const float2 x = __ffma2_rn(__fadd2_rn(y, kMinusTwo23x2), kMinusOne2, t);   // t - floor(t)
+          if constexpr (SEMB_CHECKED) {
+            const int i0 = __float_as_int(g.w) - P.tau - 0x4B000000;
+            const int t0c = min(tg.t0s + lane, P.ns - 1);
+            report_window(P.status, __float_as_int(y.x) + i0, W, src_at(c)[e], tg.cdp, t0c);
+            if (2 * rp + 1 < RC) report_window(P.status, __float_as_int(y.y) + i0, W, src_at(c)[e], tg.cdp, t0c);
+          }
           fa[2 * rp].add(min(__float_as_uint(y.x) * EB + base, top), x.x);
           if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * EB + base, top), x.y);
         }
@@ -374,6 +380,9 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
           const bool ok = (unsigned)rel <= span;
           const float x = ok ? t - (y - 8388608.0f) : 0.0f;
           const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
+          if constexpr (SEMB_CHECKED) {
+            if (ok) report_window(P.status, soff + rel, W, src_at(c)[e], tg.cdp, min(tg.t0s + lane, P.ns - 1));
+          }
           fa[r].add(bufq_addr + EB * idx, x);
           fa[r].M += ok ? 1 : 0;
         }

@@ -555,7 +555,7 @@ int semb_plan_create(const semb_params* p, int32_t device, semb_plan** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->copy_done, cudaEventDisableTiming);
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&pl->ev[i]);
-  if (e == cudaSuccess) e = cudaMalloc(&pl->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&pl->d_status, kStatusWords * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_counter, kMaxBuckets * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&pl->d_repicked, sizeof(unsigned long long));
   if (e != cudaSuccess) {
@@ -1148,7 +1148,7 @@ int enqueue_streamed(semb_plan* pl, const semb_gather_view* g) {
     pl->chunk_done.push_back(e);
   }
   SEMB_TRY(dev_reuse(pl, &pl->d_chunk_counter, nk));
-  SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, sizeof(int), st));
+  SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, kStatusWords * sizeof(int), st));
   SEMB_CUDA(cudaMemsetAsync(pl->d_chunk_counter, 0, nk * sizeof(int), st));
   SEMB_CUDA(cudaEventRecord(pl->ev[0], st));
   SEMB_CUDA(cudaStreamWaitEvent(cs, pl->ev[0], 0));
@@ -1180,9 +1180,10 @@ int enqueue_streamed(semb_plan* pl, const semb_gather_view* g) {
   ++launches;
   SEMB_CUDA(cudaEventRecord(pl->ev[3], st));
   SEMB_CUDA(cudaStreamSynchronize(st));
-  int status = 0;
+  int status_words[kStatusWords] = {};
   unsigned long long rep = 0;
-  SEMB_CUDA(cudaMemcpy(&status, pl->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  SEMB_CUDA(cudaMemcpy(status_words, pl->d_status, sizeof(status_words), cudaMemcpyDeviceToHost));
+  const int status = status_words[0];
   SEMB_CUDA(cudaMemcpy(&rep, pl->d_repicked, sizeof(rep), cudaMemcpyDeviceToHost));
   float ms = 0.f;
   SEMB_CUDA(cudaEventElapsedTime(&ms, pl->ev[0], pl->ev[3]));
@@ -1192,6 +1193,9 @@ int enqueue_streamed(semb_plan* pl, const semb_gather_view* g) {
   pl->stats.repicked = (int64_t)rep;
   pl->stats.kernel_launches = launches;
   if (status & ST_TIMEOUT) return fail(SEMB_E_TIMEOUT, "a staging wait in the search kernel timed out");
+  if (status & ST_BOUNDS)
+    return fail(SEMB_E_BOUNDS, "checked build: an item's window left its staged window (CDP %d, t0 %d, trace %d)",
+                status_words[1], status_words[2], status_words[3]);
   if (status) return fail(SEMB_E_CUDA, "search kernel reported status %d", status);
   return SEMB_OK;
 }
@@ -1374,7 +1378,7 @@ int semb_plan_run(semb_plan* pl) {
   if (!pl->uploaded) return fail(SEMB_E_STATE, "semb_plan_run before semb_plan_upload");
   SEMB_CUDA(cudaSetDevice(pl->device));
   cudaStream_t st = pl->stream;
-  SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, sizeof(int), st));
+  SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, kStatusWords * sizeof(int), st));
   const bool chunked = pl->chunk_cdps > 0 && pl->p.mode == SEMB_BATCHED && pl->p.ngen == 0 &&
                        pl->ns >= 2 * pl->tau + 2;
   pl->chunk_ms.clear();
@@ -1402,9 +1406,10 @@ int semb_plan_run(semb_plan* pl) {
     SEMB_TRY(enqueue_run(pl, true));
   }
   SEMB_CUDA(cudaStreamSynchronize(st));
-  int status = 0;
+  int status_words[kStatusWords] = {};
   unsigned long long rep = 0;
-  SEMB_CUDA(cudaMemcpy(&status, pl->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  SEMB_CUDA(cudaMemcpy(status_words, pl->d_status, sizeof(status_words), cudaMemcpyDeviceToHost));
+  const int status = status_words[0];
   if (pl->p.mode == SEMB_BATCHED)
     SEMB_CUDA(cudaMemcpy(&rep, pl->d_repicked, sizeof(rep), cudaMemcpyDeviceToHost));
   // graph replays are timed as a whole; the per-kernel split needs direct launches
@@ -1425,6 +1430,9 @@ int semb_plan_run(semb_plan* pl) {
   pl->stats.ms_total = c;
   pl->stats.repicked = (int64_t)rep;
   if (status & ST_TIMEOUT) return fail(SEMB_E_TIMEOUT, "a staging wait in the search kernel timed out");
+  if (status & ST_BOUNDS)
+    return fail(SEMB_E_BOUNDS, "checked build: an item's window left its staged window (CDP %d, t0 %d, trace %d)",
+                status_words[1], status_words[2], status_words[3]);
   if (status) return fail(SEMB_E_CUDA, "search kernel reported status %d", status);
   return SEMB_OK;
 }

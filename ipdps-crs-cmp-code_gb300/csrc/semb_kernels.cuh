@@ -70,8 +70,20 @@ constexpr int kGlobalEntry = INT32_MIN;
 constexpr int kMaxThreads = 256; // CTA size limit of the search kernel (variants use 128 or 256)
 constexpr uint64_t kWaitNs = 2000000000ull;  // bounded mbarrier wait (2 s), then error
 
-// Device status word bits.
-enum { ST_TIMEOUT = 1, ST_BAD_ARG = 2 };
+// Device status words: [0] bits, [1..3] the first bounds violation of a checked build
+// (CDP, t0, trace).
+enum { ST_TIMEOUT = 1, ST_BAD_ARG = 2, ST_BOUNDS = 4 };
+constexpr int kStatusWords = 4;
+
+// Checked build (compiled with -DSEMB_CHECKED=1 into libsemb_gb300_checked.so): every
+// item that reads a staged window is tested against the window its trace was staged
+// with, the property the planner's bounds guarantee (the unchecked kernels rely on it
+// and only clamp addresses to the buffer as a guard).  A violation sets ST_BOUNDS and
+// records the first offender; the address stays clamped, so nothing outside the
+// buffer is read and the search runs to its end.
+#ifndef SEMB_CHECKED
+#define SEMB_CHECKED 0
+#endif
 
 struct KParams {
   // trace store, [ntr][pitch]; pitch is a multiple of 8 elements with at least 8
@@ -167,6 +179,18 @@ __device__ __forceinline__ float sqrt_fast(float x) {
 
 __device__ __forceinline__ float half_bits_to_float(uint32_t b) {
   return __half2float(__ushort_as_half(static_cast<unsigned short>(b)));
+}
+
+// Checked build: the window samples idx .. idx + W of an item must lie inside the
+// staged window [off, off + len) of its entry (src = (trace, lo, len, off), buffer
+// units); the first violation is recorded with its CDP, t0 and trace.
+static __device__ __noinline__ void report_window(int* status, int idx, int W, int4 src, int cdp, int t0) {
+  if (idx >= src.w && idx + W <= src.w + src.z - 1) return;
+  if ((atomicOr(status, ST_BOUNDS) & ST_BOUNDS) == 0) {
+    status[1] = cdp;
+    status[2] = t0;
+    status[3] = src.x;
+  }
 }
 
 // Pick order: larger semblance first; equal semblance -> lower grid index first.
@@ -903,7 +927,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
 
       // compute on a staged chunk (meta, n); the fast form then folds the chunk's
       // energy into the Kahan totals
-      auto compute_chunk = [&](const ChunkMeta* meta, const int n) {
+      auto compute_chunk = [&](const ChunkMeta* meta, const int n, const int4* srcc) {
         if (FORM == FORM_PLAIN) {
           for (int e = 0; e < n; ++e) {
             const float4 g = meta->geo[e];
@@ -924,6 +948,9 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
               const int it = __float_as_int(y) - 0x4B000000;
               const float x = ok ? __fsub_rn(t, __fsub_rn(y, 8388608.0f)) : 0.0f;
               const unsigned idx = min(ok ? (unsigned)(soff + it - P.tau) : (unsigned)P.cap, (unsigned)P.cap);
+              if constexpr (SEMB_CHECKED) {
+                if (ok) report_window(P.status, soff + it - P.tau, W, srcc[e], cdp, t0);
+              }
               const float* s = buf + idx;
               float s1 = s[0];
 #pragma unroll
@@ -969,6 +996,11 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
               const float2 t = make_float2(sqrt_fast(t2.x), sqrt_fast(t2.y));
               const float2 y = __fadd2_rz(t, kTwo23x2);
               const float2 x = __ffma2_rn(__fadd2_rn(y, kMinusTwo23x2), kMinusOne2, t);   // t - floor(t)
+              if constexpr (SEMB_CHECKED) {
+                const int i0 = __float_as_int(g.w) - P.tau - 0x4B000000;
+                report_window(P.status, __float_as_int(y.x) + i0, W, srcc[e], cdp, t0);
+                if (2 * rp + 1 < RC) report_window(P.status, __float_as_int(y.y) + i0, W, srcc[e], cdp, t0);
+              }
               fa[2 * rp].add(min(__float_as_uint(y.x) * 16u + base, top), x.x);
               if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * 16u + base, top), x.y);
             }
@@ -1004,6 +1036,9 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
               const bool ok = (unsigned)rel <= span;
               const float x = ok ? t - (y - 8388608.0f) : 0.0f;
               const unsigned idx = min(ok ? (unsigned)(soff + rel) : (unsigned)P.cap, (unsigned)P.cap);
+              if constexpr (SEMB_CHECKED) {
+                if (ok) report_window(P.status, soff + rel, W, srcc[e], cdp, t0);
+              }
               fa[r].add(bufq_addr + 16u * idx, x);
               fa[r].M += ok ? 1 : 0;
             }
@@ -1040,7 +1075,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
             return;
           }
           const int consumed = meta->consumed;
-          compute_chunk(meta, n);
+          compute_chunk(meta, n, srcinfo);
           ap_pos += consumed;
           __syncthreads();   // buffer and meta free for the next chunk
         }
@@ -1074,7 +1109,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
               issue_raw(P, mn, srcs + (cur ^ 1) * kMaxChunk, raw_at(cur ^ 1), bars + (cur ^ 1));
             }
           }
-          compute_chunk(mc, n);
+          compute_chunk(mc, n, srcs + cur * kMaxChunk);
           __syncthreads();   // quad buffer free; the next chunk's metadata visible
           ap_pos = next;
           cur ^= 1;

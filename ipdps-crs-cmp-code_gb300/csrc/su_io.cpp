@@ -412,6 +412,7 @@ const char* semb_strerror(int code) {
     case SEMB_E_TIMEOUT: return "device wait timed out";
     case SEMB_E_STATE: return "call out of order";
     case SEMB_E_NODEV: return "no usable CUDA device";
+    case SEMB_E_BOUNDS: return "bounds check failed (checked build)";
     default: return "unknown error";
   }
 }

@@ -22,7 +22,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libsemb_gb300.so")
+# SEMB_CHECKED=1 in the environment selects the bounds-checked build of the same ABI
+LIB_PATH = os.path.join(HERE, "_build", "libsemb_gb300_checked.so" if os.environ.get("SEMB_CHECKED") == "1"
+                        else "libsemb_gb300.so")
 
 CMP, CRS = 0, 1
 PLAIN_F32, BATCHED = 0, 1
@@ -33,7 +35,7 @@ ABI_VERSION = 8
 MAX_VARIANTS = 24   # SEMB_MAX_VARIANTS
 MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
-OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODEV = range(10)
+OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODEV, E_BOUNDS = range(11)
 
 EXPORTS = [
     "semb_params_init", "semb_survey_load", "semb_survey_from_bytes", "semb_survey_view", "semb_survey_write",
