@@ -318,11 +318,14 @@ int semb_plan_buckets(const semb_plan* plan, int32_t* nbuckets, int32_t* ap_lo, 
 int semb_plan_set_variant(semb_plan* plan, int32_t variant);
 
 /* Batched form: stage at most max_samples window samples per chunk in shared memory
- * (0, the default: as much as the kernel variant's resident CTAs per SM leave, at
- * least 512).  A trace whose window is larger than the stage is read from the FP32
- * store in global memory instead; results are those of the staged path (bit for bit
- * with SEMB_STORE_F32).  Smaller stages let more CTAs share an SM.  Takes effect at
- * once on an uploaded plan.  No counterpart in the reference. */
+ * (0, the default: as much as the kernel variant's resident CTAs per SM leave).
+ * Applies to the variants built with a global-memory path (16-18), whose stages may
+ * be smaller than a trace (at least 512 samples by default): a trace whose window is
+ * larger than the stage is read from the FP32 store in global memory instead, with
+ * the staged path's arithmetic (with SEMB_STORE_F32 the results differ only by the
+ * order of FP32 sums).  The other variants always stage whole windows.  Smaller
+ * stages let more CTAs share an SM.  Takes effect at once on an uploaded plan.  No
+ * counterpart in the reference. */
 int semb_plan_set_staging(semb_plan* plan, int32_t max_samples);
 
 /* Batched grid search in chunks of cdps_per_chunk contiguous CDPs (0, the default:

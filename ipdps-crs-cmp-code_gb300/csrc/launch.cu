@@ -17,7 +17,8 @@ static SearchEntry lookup(int method, int form, int w, int v) {
   return form == FORM_PLAIN ? search_entry_crs_plain(w, v) : search_entry_crs_fast(w, v);
 }
 
-int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt, int* pipe, int* lay) {
+int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt, int* pipe, int* lay,
+                   int* glob) {
   if (v < 0 || v >= kMaxVariants) return 0;
   SearchEntry e = lookup(method, form, w, v);
   *rc = e.rc;
@@ -26,6 +27,7 @@ int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* 
   *nt = e.nt;
   if (pipe) *pipe = e.pipe;
   if (lay) *lay = e.lay;
+  if (glob) *glob = e.glob;
   return e.fn != nullptr;
 }
 

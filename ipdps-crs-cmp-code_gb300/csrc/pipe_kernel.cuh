@@ -93,7 +93,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 
 // TU: unroll factor of the in-range trace loop (independent work of TU traces in
 // flight per iteration).
-template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TU = 1>
+// GLOB: as for semb_search_kernel, the variant may stage less than a whole trace.
+template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TU = 1, bool GLOB = false>
 __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT, LAY);
@@ -358,7 +359,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
           const float u0 = fmaf(CA(0), g.x, Tsmp);
           q0 = fmaf(u0, u0, CC(0) * g.z);
         }
-        if (soff == kGlobalEntry) {
+        if (GLOB && soff == kGlobalEntry) {
           // a window larger than a stage: the items read the FP32 store
           global_entry<METHOD, BRUN>(P, meta->raw[e], g, q0, Tsmp, T2smp, span, ca2, cb2, cc2, fa);
           continue;

@@ -29,7 +29,7 @@ namespace semb {
 int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
 int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt, int* pipe,
-                   int* lay);
+                   int* lay, int* glob = nullptr);
 constexpr int kVariantSlots = SEMB_MAX_VARIANTS;
 constexpr int kMaxBuckets = SEMB_MAX_BUCKETS;
 // aperture split points of the work queue (traces): buckets > 1024, 385-1024,
@@ -364,8 +364,8 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
 int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0, lay = 0;
-  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe, &lay))
+  int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0, lay = 0, glob = 0;
+  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe, &lay, &glob))
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
   const int ncand = pl->ncand;
   // search order; a negative slot -1-g marks padding that repeats candidate g.
@@ -401,11 +401,13 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
 
   // staging capacity, shared memory and residency, checked before the plan's
   // device state changes (a variant that does not fit leaves the plan as it was)
-  // The plain form stages whole windows always (capacity >= one trace).  The batched
-  // form reads a window larger than its staging capacity from the FP32 store in
-  // global memory (kGlobalEntry), so its stages need not hold a whole trace: the
-  // capacity is what the variant's resident CTAs per SM leave, at least kMinStage
-  // samples (or the plan's stage_cap, which also bounds it from above).
+  // Variants without the global path (glob = 0, every plain variant) stage whole
+  // windows always (capacity >= one trace).  A batched variant with it reads a window
+  // larger than its staging capacity from the FP32 store in global memory
+  // (kGlobalEntry), so its stages need not hold a whole trace: the capacity is what
+  // the variant's resident CTAs per SM leave, at least kMinStage samples (or the
+  // plan's stage_cap, which also bounds it from above).
+  const bool small_stages = form == FORM_FAST && glob;
   const int store = (form == FORM_FAST) ? p.storage : SEMB_STORE_F32;
   const size_t budget = (227 * 1024) / minb - 1024;
   int cap = form == FORM_PLAIN ? 32768 : 8192;
@@ -415,7 +417,7 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   };
   while (cap > 64 && smem_of(cap) > budget) cap -= 64;
   int min_cap = (int)pl->pitch + 16;
-  if (form == FORM_FAST) min_cap = std::min(min_cap, pl->stage_cap > 0 ? pl->stage_cap : kMinStage);
+  if (small_stages) min_cap = std::min(min_cap, pl->stage_cap > 0 ? pl->stage_cap : kMinStage);
   if (cap < min_cap) cap = (min_cap + 63) & ~63;
   const size_t smem = smem_of(cap);
   if (smem > 227 * 1024) return fail(SEMB_E_ARG, "ns %d too large for the staging buffer", pl->ns);

@@ -31,18 +31,23 @@ struct SearchEntry {
   int nt;     // threads per CTA
   int pipe;   // 1: semb_pipe_kernel (decoupled staging ring), 0: semb_search_kernel
   int lay;    // staging layout (LAY_*)
+  int glob;   // 1: stages may be smaller than a trace (long windows read global memory)
 };
 
 constexpr int kMaxVariants = SEMB_MAX_VARIANTS;
 
-template <int METHOD, int FORM, int W, int RC, int MINB, int LAY = LAY_QUAD, bool BRUN = false, int NT = 256>
+template <int METHOD, int FORM, int W, int RC, int MINB, int LAY = LAY_QUAD, bool BRUN = false, int NT = 256,
+          bool GLOB = false>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT>, RC, MINB, BRUN ? 1 : 0, NT, 0, LAY};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT, GLOB>, RC, MINB, BRUN ? 1 : 0, NT,
+          0, LAY, GLOB ? 1 : 0};
 }
 
-template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256, int TU = 1>
+template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256, int TU = 1,
+          bool GLOB = false>
 SearchEntry pipe_entry() {
-  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT, TU>, RC, MINB, BRUN ? 1 : 0, NT, 1, LAY};
+  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT, TU, GLOB>, RC, MINB, BRUN ? 1 : 0, NT, 1, LAY,
+          GLOB ? 1 : 0};
 }
 
 // Plain form: one variant per window.
@@ -55,7 +60,7 @@ SearchEntry plain_entry() {
 template <int METHOD, int FORM>
 SearchEntry search_entry(int w, int variant) {
   if constexpr (FORM == FORM_PLAIN) {
-    if (variant != 0) return {nullptr, 0, 0, 0, 0, 0, 0};
+    if (variant != 0) return {nullptr, 0, 0, 0, 0, 0, 0, 0};
     switch (w) {
       case 1: return plain_entry<METHOD, 1>();
       case 3: return plain_entry<METHOD, 3>();
@@ -67,7 +72,7 @@ SearchEntry search_entry(int w, int variant) {
       case 13: return plain_entry<METHOD, 13>();
       case 15: return plain_entry<METHOD, 15>();
 #endif
-      default: return {nullptr, 0, 0, 0, 0, 0, 0};
+      default: return {nullptr, 0, 0, 0, 0, 0, 0, 0};
     }
   } else {
   // fast form
@@ -101,9 +106,13 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 15) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
       // stages smaller than a trace (windows beyond them read from global memory):
       // two 256-thread CTAs per SM, and 640 threads of 6 candidates
-      if (variant == 16) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 2, LAY_PD, METHOD == METHOD_CRS, 256, 2>();
-      if (variant == 17) return pipe_entry<METHOD, 3, 6, 1, LAY_PD, METHOD == METHOD_CRS, 640>();
-      if (variant == 18) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 2, LAY_P2, METHOD == METHOD_CRS, 256>();
+      if (variant == 16) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 2, LAY_PD, METHOD == METHOD_CRS, 256, 2, true>();
+      if (variant == 17) return pipe_entry<METHOD, 3, 6, 1, LAY_PD, METHOD == METHOD_CRS, 640, 1, true>();
+      if (variant == 18) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 2, LAY_P2, METHOD == METHOD_CRS, 256, 1, true>();
+      // the packed layouts with the pair's samples formed by scalar FMAs
+      if (variant == 19) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_P2S, METHOD == METHOD_CRS, 512>();
+      if (variant == 20) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PDS, METHOD == METHOD_CRS, 512, 2>();
+      if (variant == 21) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2S>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -122,9 +131,12 @@ SearchEntry search_entry(int w, int variant) {
       if (METHOD == METHOD_CRS && variant == 14) return pipe_entry<METHOD, 5, 7, 1, LAY_P2, true, 512>();
       if (variant == 15) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_QUAD, METHOD == METHOD_CRS, 512>();
       // stages smaller than a trace: two 256-thread CTAs per SM
-      if (variant == 16) return pipe_entry<METHOD, 5, 7, 2, LAY_P2, METHOD == METHOD_CRS, 256>();
-      if (variant == 17) return pipe_entry<METHOD, 5, 6, 2, LAY_SD, METHOD == METHOD_CRS, 256>();
-      if (variant == 18) return pipe_entry<METHOD, 5, 7, 2, LAY_QUAD, METHOD == METHOD_CRS, 256>();
+      if (variant == 16) return pipe_entry<METHOD, 5, 7, 2, LAY_P2, METHOD == METHOD_CRS, 256, 1, true>();
+      if (variant == 17) return pipe_entry<METHOD, 5, 6, 2, LAY_SD, METHOD == METHOD_CRS, 256, 1, true>();
+      if (variant == 18) return pipe_entry<METHOD, 5, 7, 2, LAY_QUAD, METHOD == METHOD_CRS, 256, 1, true>();
+      if (variant == 19) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_P2S, METHOD == METHOD_CRS, 512>();
+      if (variant == 20) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_P2S, METHOD == METHOD_CRS, 128>();
+      if (variant == 21) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2S>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;
@@ -135,7 +147,7 @@ SearchEntry search_entry(int w, int variant) {
 #endif
     default: break;
   }
-  return {nullptr, 0, 0, 0, 0, 0, 0};
+  return {nullptr, 0, 0, 0, 0, 0, 0, 0};
   }
 }
 

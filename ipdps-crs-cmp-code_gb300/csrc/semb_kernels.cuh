@@ -206,6 +206,16 @@ constexpr int LAY_QUAD = 0;   // (s_k, s_k+1, s_k+2, s_k+3)
 constexpr int LAY_SD = 1;     // (s_k, s_k+1 - s_k, s_k+1, s_k+2 - s_k+1)
 constexpr int LAY_P2 = 2;     // (s_k, s_k+2, s_k+1, s_k+3)
 constexpr int LAY_PD = 3;     // w = 3: (s_k, s_k+2, s_k+1 - s_k, s_k+3 - s_k+2)
+// The same staged entries as LAY_P2 / LAY_PD; the items form the two interpolated
+// samples of a pair with scalar FMAs into one register pair instead of a packed
+// FP32x2 FMA, whose weight operand (x, x) costs register moves per item.
+constexpr int LAY_P2S = 4;
+constexpr int LAY_PDS = 5;
+
+// layout of the staged entries of an accumulation layout
+__host__ __device__ constexpr int stage_lay(int lay) {
+  return lay == LAY_P2S ? LAY_P2 : lay == LAY_PDS ? LAY_PD : lay;
+}
 
 // bytes of one staged entry
 __host__ __device__ constexpr int lay_entry_bytes(int) { return 16; }
@@ -481,9 +491,10 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
           v[u] = (f16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
         }
       }
-      dst[k] = LAY == LAY_SD   ? make_float4(v[0], v[1] - v[0], v[1], v[2] - v[1])
-               : LAY == LAY_P2 ? make_float4(v[0], v[2], v[1], v[3])
-               : LAY == LAY_PD ? make_float4(v[0], v[2], v[1] - v[0], v[3] - v[2])
+      constexpr int SL = stage_lay(LAY);
+      dst[k] = SL == LAY_SD   ? make_float4(v[0], v[1] - v[0], v[1], v[2] - v[1])
+               : SL == LAY_P2 ? make_float4(v[0], v[2], v[1], v[3])
+               : SL == LAY_PD ? make_float4(v[0], v[2], v[1] - v[0], v[3] - v[2])
                                : make_float4(v[0], v[1], v[2], v[3]);
     }
   }
@@ -617,8 +628,8 @@ struct FastAcc {
 // with lo = (s_j, s_j+2), hi = (s_j+1, s_j+3).  Window samples 4q..4q+3 use
 // entries k+4q (pairs (4q, 4q+2)) and k+4q+2 (pairs (4q+1, 4q+3)); the one
 // sample left over (W is odd) is done in scalar arithmetic.
-template <int W>
-struct FastAcc<W, LAY_P2> {
+template <int W, bool SV>
+struct P2Acc {
   static constexpr int NP = (W - 1) / 2 > 0 ? (W - 1) / 2 : 1;
   float2 np[NP];   // packed sums (num_j, num_j+2)
   float ns;        // sum of the unpaired window sample
@@ -634,7 +645,7 @@ struct FastAcc<W, LAY_P2> {
   }
   __device__ __forceinline__ void pair(int i, float2 lo, float2 hi, float2 xx) {
     const float2 d = __ffma2_rn(lo, make_float2(-1.f, -1.f), hi);   // hi - lo, exact as a subtraction
-    const float2 v = __ffma2_rn(d, xx, lo);
+    const float2 v = SV ? make_float2(fmaf(d.x, xx.x, lo.x), fmaf(d.y, xx.x, lo.y)) : __ffma2_rn(d, xx, lo);
     np[i] = __fadd2_rn(np[i], v);
     den2 = __ffma2_rn(v, v, den2);
   }
@@ -706,12 +717,17 @@ struct FastAcc<W, LAY_P2> {
   }
 };
 
+template <int W>
+struct FastAcc<W, LAY_P2> : P2Acc<W, false> {};
+template <int W>
+struct FastAcc<W, LAY_P2S> : P2Acc<W, true> {};
+
 // Packed values with their differences (w = 3): entry k = (s_k, s_k+2, d_k, d_k+2),
 // d_j = s_j+1 - s_j.  Window samples 0 and 2 are one FP32x2 FMA without forming the
 // differences; sample 1 takes s_1 = s_0 + d_0 (within a rounding of the stored value)
 // and d_1 = s_2 - s_1.
-template <int W>
-struct FastAcc<W, LAY_PD> {
+template <int W, bool SV>
+struct PDAcc {
   static_assert(W == 3, "the packed value/difference layout is for w = 3");
   float2 np;     // (num_0, num_2)
   float ns;      // num_1
@@ -730,7 +746,8 @@ struct FastAcc<W, LAY_PD> {
     acc(make_float4(sv[0], sv[2], sv[1] - sv[0], sv[3] - sv[2]), x);
   }
   __device__ __forceinline__ void acc(const float4 A, float x) {   // A = (s_0, s_2, d_0, d_2)
-    const float2 v = __ffma2_rn(make_float2(A.z, A.w), make_float2(x, x), make_float2(A.x, A.y));
+    const float2 v = SV ? make_float2(fmaf(A.z, x, A.x), fmaf(A.w, x, A.y))
+                        : __ffma2_rn(make_float2(A.z, A.w), make_float2(x, x), make_float2(A.x, A.y));
     np = __fadd2_rn(np, v);
     den2 = __ffma2_rn(v, v, den2);
     const float s1 = A.x + A.z;
@@ -748,6 +765,11 @@ struct FastAcc<W, LAY_PD> {
     lin = np.x + np.y + ns;
   }
 };
+
+template <int W>
+struct FastAcc<W, LAY_PD> : PDAcc<W, false> {};
+template <int W>
+struct FastAcc<W, LAY_PDS> : PDAcc<W, true> {};
 
 
 
@@ -790,7 +812,11 @@ __device__ __forceinline__ void global_entry(const KParams& P, int tr, float4 g,
 // ---------------------------------------------------------------------------
 // The search kernel.
 
-template <int METHOD, int FORM, int W, int RC, int MINB, int LAY, bool BRUN, int NT>
+// GLOB: the variant may stage less than a whole trace; windows larger than its
+// buffer are read from the FP32 store (kGlobalEntry).  Without it the plan gives
+// the variant a buffer that holds any window, and the path is not compiled (it
+// costs registers in the partly-in-range loop).
+template <int METHOD, int FORM, int W, int RC, int MINB, int LAY, bool BRUN, int NT, bool GLOB = false>
 __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage, NT);
@@ -1015,7 +1041,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
               const float u0 = fmaf(CA(0), g.x, Tsmp);
               q0 = fmaf(u0, u0, CC(0) * g.z);
             }
-            if (soff == kGlobalEntry) {
+            if (GLOB && soff == kGlobalEntry) {
               global_entry<METHOD, BRUN>(P, meta->raw[e], g, q0, Tsmp, T2smp, span, ca2, cb2, cc2, fa);
               continue;
             }

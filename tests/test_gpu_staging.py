@@ -6,9 +6,10 @@ FP32 store in global memory instead, with the same arithmetic.  These surveys ha
 windows of hundreds to over a thousand samples (a pass spans the whole velocity or
 C range at offsets up to 3 km), and the plans are forced to stages of 64-256
 samples, so most far-offset traces take the global path.  With FP32 storage the
-staged entries hold exactly the FP32 samples, so the results must be bit-identical
-to the default staging; with FP16 storage they must stay within the batched form's
-error of the FP64 oracle."""
+staged entries hold exactly the FP32 samples, so the results equal the default
+staging's up to the order of the FP32 sums (smaller stages cut a pass into more
+chunks, and a chunk's in-range traces are summed before its others); with FP16
+storage they must stay within the batched form's error of the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -37,7 +38,7 @@ def _gather(kind, s, real=np.float32):
 
 
 @pytest.mark.parametrize("case", [0, 1])
-def test_small_stages_are_bit_identical_with_fp32_storage(case):
+def test_small_stages_match_the_default_staging_with_fp32_storage(case):
     kind, method, s = _surveys()[case]
     g = _gather(kind, s)
     with semb.Plan(semb.params(method, mode=semb.BATCHED, storage=semb.STORE_F32, repick=semb.REPICK_OFF,
@@ -53,9 +54,10 @@ def test_small_stages_are_bit_identical_with_fp32_storage(case):
             for cap in (256, 64):
                 plan.set_staging(cap)
                 plan.run()
-                out = plan.download()
-                for a, b in zip(out, ref):
-                    assert np.array_equal(a, b), (v, cap)
+                ctr, sem, stk = plan.download()
+                assert np.mean(ctr == ref[0]) >= 0.999, (v, cap)
+                np.testing.assert_allclose(sem, ref[1], rtol=1e-5, atol=1e-6, err_msg=f"{v} {cap}")
+                np.testing.assert_allclose(stk, ref[2], rtol=1e-5, atol=1e-6, err_msg=f"{v} {cap}")
 
 
 def _has(plan, v):
