@@ -31,13 +31,17 @@ int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* 
   return e.fn != nullptr;
 }
 
-// Variant a plan starts with (before any autotuning): for CRS the pipelined
-// 512-thread B-run kernel, the fastest on the CRS workloads measured on GB300 (with
-// the packed value/difference staging for w = 3); for CMP the two-barrier kernel's
-// variant 0.
+// Variant a plan starts with (before any autotuning), the fastest measured on GB300
+// for the benchmark workloads of each window: for CRS the pipelined 512-thread B-run
+// kernel (packed value/difference staging with a two-way trace unroll for w = 3,
+// packed pairs otherwise); for CMP the two-barrier kernel with packed pairs (w = 3)
+// or packed pairs formed by scalar FMAs (w = 5); variant 0 elsewhere.
 int default_variant(int method, int form, int w) {
-  if (method == METHOD_CRS && form == FORM_FAST && w == 3) return 13;
-  if (method == METHOD_CRS && form == FORM_FAST && w <= 5) return 14;
+  if (form != FORM_FAST) return 0;
+  if (method == METHOD_CRS && w == 3) return 13;
+  if (method == METHOD_CRS && w <= 5) return 14;
+  if (method == METHOD_CMP && w == 3) return 8;
+  if (method == METHOD_CMP && w == 5) return 21;
   return 0;
 }
 

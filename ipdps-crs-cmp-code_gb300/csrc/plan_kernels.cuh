@@ -478,14 +478,15 @@ static __global__ void k_repick(RepickParams R) {
     }
     if (lane == 0) atomicAdd(R.repicked, 1ull);
   } else if (redo) {
-    double num[kTopK][W], den[kTopK], lin[kTopK];
+    // sums per candidate; the stack's linear sum is taken as the sum of the window
+    // numerators at the end (the same quantity, summed in another order)
+    double num[kTopK][W], den[kTopK];
     int M[kTopK];
 #pragma unroll
     for (int q = 0; q < kTopK; ++q) {
 #pragma unroll
       for (int j = 0; j < W; ++j) num[q][j] = 0.0;
       den[q] = 0.0;
-      lin[q] = 0.0;
       M[q] = 0;
     }
     double pa[kTopK], pb[kTopK], pc[kTopK];
@@ -524,7 +525,6 @@ static __global__ void k_repick(RepickParams R) {
             const double v = (s1 - s0) * x + s0;
             num[q][j] += v;
             den[q] += v * v;
-            lin[q] += v;
           }
           ++M[q];
         }
@@ -537,7 +537,6 @@ static __global__ void k_repick(RepickParams R) {
 #pragma unroll
         for (int j = 0; j < W; ++j) num[q][j] += __shfl_xor_sync(0xffffffffu, num[q][j], o);
         den[q] += __shfl_xor_sync(0xffffffffu, den[q], o);
-        lin[q] += __shfl_xor_sync(0xffffffffu, lin[q], o);
         M[q] += __shfl_xor_sync(0xffffffffu, M[q], o);
       }
     }
@@ -547,12 +546,15 @@ static __global__ void k_repick(RepickParams R) {
 #pragma unroll
     for (int q = 0; q < kTopK; ++q) {
       if (ti[q] < 0) continue;
-      double acsq = 0.0;
+      double acsq = 0.0, lin = 0.0;
 #pragma unroll
-      for (int j = 0; j < W; ++j) acsq += num[q][j] * num[q][j];
+      for (int j = 0; j < W; ++j) {
+        acsq += num[q][j] * num[q][j];
+        lin += num[q][j];
+      }
       const bool ok = den[q] > 1e-13 && M[q] > 0 && (napert - M[q]) < 2;
       const double sem = ok ? acsq / (den[q] * (double)M[q]) : 0.0;
-      const double stk = ok ? lin[q] / ((double)W * (double)M[q]) : 0.0;
+      const double stk = ok ? lin / ((double)W * (double)M[q]) : 0.0;
       if (sem > 0.0 && (sem > bs || (sem == bs && ti[q] < bi))) {
         bs = sem;
         bi = ti[q];
