@@ -80,7 +80,7 @@ __host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, 
   L.tops = L.src + (size_t)kMetaRing * kMaxChunk * 16;
   L.kahan = L.tops + align128(3 * (size_t)kTopK * nt * 4);
   L.quad = L.kahan + align128(2 * (size_t)rc * nt * 4);
-  L.quad_stride = align128(((size_t)cap + kZeroSlots) * lay_entry_bytes(lay));
+  L.quad_stride = align128(((size_t)cap + kZeroSlots) * lay_stage_bytes(lay));
   L.raw = L.quad + kStages * L.quad_stride;
   L.raw_stride = align128(((size_t)cap + 8 * kMaxChunk) * (storage == STORE_F32 ? 4 : 2));
   L.total = L.raw + kRawBufs * L.raw_stride;
@@ -126,9 +126,12 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   const int nwarps = blockDim.x >> 5;
   constexpr float kSent = (METHOD == METHOD_CMP) ? -1.0f : 0.0f;
 
-  for (int s = 0; s < kStages; ++s)
+  for (int s = 0; s < kStages; ++s) {
     if (threadIdx.x < kZeroSlots * (EB / 16))
       quad_at(s)[P.cap * (EB / 16) + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (LAY == LAY_FT && threadIdx.x < kZeroSlots)   // the side entries' zero block
+      reinterpret_cast<float2*>(quad_at(s) + P.cap + kZeroSlots)[P.cap + threadIdx.x] = make_float2(0.f, 0.f);
+  }
   if (threadIdx.x == 0) {
     for (int b = 0; b < kRawBufs; ++b) mbar_init(&raw_full[b], 1);
     for (int s = 0; s < kStages; ++s) {
@@ -308,6 +311,8 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
       const int n = meta->n, n_in = meta->n_in;
       const uint32_t bufq_addr = smem_u32(quad_at(c));
       const uint32_t top = bufq_addr + EB * (uint32_t)P.cap;
+      // LAY_FT: side entry address of main entry address a is a / 2 + side_shift
+      const uint32_t side_shift = bufq_addr + 16u * (uint32_t)(P.cap + kZeroSlots) - (bufq_addr >> 1);
       const float2 Tsmp2 = make_float2(Tsmp, Tsmp);
       const float2 T2smp2 = make_float2(T2smp, T2smp);
       // traces on which every item is in range: traveltimes of item pairs in
@@ -345,8 +350,18 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
             report_window(P.status, __float_as_int(y.x) + i0, W, src_at(c)[e], tg.cdp, t0c);
             if (2 * rp + 1 < RC) report_window(P.status, __float_as_int(y.y) + i0, W, src_at(c)[e], tg.cdp, t0c);
           }
-          fa[2 * rp].add(min(__float_as_uint(y.x) * EB + base, top), x.x);
-          if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * EB + base, top), x.y);
+          if constexpr (LAY == LAY_FT) {
+            // main entry a (16 bytes per sample), side entry a / 2 + side_shift (8 bytes)
+            const uint32_t a0 = min(__float_as_uint(y.x) * EB + base, top);
+            fa[2 * rp].add_ft(a0, (a0 >> 1) + side_shift, t.x);
+            if (2 * rp + 1 < RC) {
+              const uint32_t a1 = min(__float_as_uint(y.y) * EB + base, top);
+              fa[2 * rp + 1].add_ft(a1, (a1 >> 1) + side_shift, t.y);
+            }
+          } else {
+            fa[2 * rp].add(min(__float_as_uint(y.x) * EB + base, top), x.x);
+            if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * EB + base, top), x.y);
+          }
         }
       }
       // the other traces: per-item range checks; an out-of-range item reads the
@@ -384,7 +399,12 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
           if constexpr (SEMB_CHECKED) {
             if (ok) report_window(P.status, soff + rel, W, src_at(c)[e], tg.cdp, min(tg.t0s + lane, P.ns - 1));
           }
-          fa[r].add(bufq_addr + EB * idx, x);
+          if constexpr (LAY == LAY_FT) {
+            const uint32_t a = bufq_addr + EB * idx;
+            fa[r].add_ft(a, (a >> 1) + side_shift, ok ? t : 0.0f);
+          } else {
+            fa[r].add(bufq_addr + EB * idx, x);
+          }
           fa[r].M += ok ? 1 : 0;
         }
       }

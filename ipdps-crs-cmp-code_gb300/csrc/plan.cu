@@ -367,6 +367,8 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0, lay = 0, glob = 0;
   if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe, &lay, &glob))
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
+  if (lay == LAY_FT && pl->ns > kMaxNsFT)
+    return fail(SEMB_E_ARG, "variant %d (pre-offset values) is for ns <= %d", v, kMaxNsFT);
   const int ncand = pl->ncand;
   // search order; a negative slot -1-g marks padding that repeats candidate g.
   // B-run variants pad each (A, C) group's run of nb B values to a multiple of RC

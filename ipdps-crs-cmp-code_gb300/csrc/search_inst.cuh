@@ -113,6 +113,9 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 19) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_P2S, METHOD == METHOD_CRS, 512>();
       if (variant == 20) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PDS, METHOD == METHOD_CRS, 512, 2>();
       if (variant == 21) return entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2S>();
+      // pre-offset values: no per-item interpolation weight (24 staged bytes per sample)
+      if (variant == 22) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_FT, METHOD == METHOD_CRS, 512, 2>();
+      if (variant == 23) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_FT, METHOD == METHOD_CRS, 512>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();

@@ -211,14 +211,25 @@ constexpr int LAY_PD = 3;     // w = 3: (s_k, s_k+2, s_k+1 - s_k, s_k+3 - s_k+2)
 // FP32x2 FMA, whose weight operand (x, x) costs register moves per item.
 constexpr int LAY_P2S = 4;
 constexpr int LAY_PDS = 5;
+// w = 3, pipelined kernel only: values pre-offset by their window's integer sample,
+// F_k,j = s_k+j - (k + tau) d_k+j with d_m = s_m+1 - s_m, so that an item at
+// traveltime t (samples) interpolates v_j = F_k,j + t d_k+j with no weight t - floor(t):
+// a 16-byte entry (F_k,0, F_k,2, d_k, d_k+2) and an 8-byte side entry (F_k,1, d_k+1)
+// per window start k, 24 bytes per sample.  The pre-offset costs precision in
+// proportion to the sample index (about ns x 2^-24 of |d|), so plans use it for
+// ns <= 8192 only.
+constexpr int LAY_FT = 6;
+constexpr int kMaxNsFT = 8192;
 
 // layout of the staged entries of an accumulation layout
 __host__ __device__ constexpr int stage_lay(int lay) {
   return lay == LAY_P2S ? LAY_P2 : lay == LAY_PDS ? LAY_PD : lay;
 }
 
-// bytes of one staged entry
+// bytes of one staged entry (the address stride of an item's window), and of one
+// staged sample with its side entry (LAY_FT)
 __host__ __device__ constexpr int lay_entry_bytes(int) { return 16; }
+__host__ __device__ constexpr int lay_stage_bytes(int lay) { return lay == LAY_FT ? 24 : 16; }
 
 struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
@@ -480,6 +491,27 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
     const float* r32 = reinterpret_cast<const float*>(raw) + roff;
     const uint16_t* r16 = reinterpret_cast<const uint16_t*>(raw) + roff;
     const bool f16 = P.storage == STORE_F16;
+    if constexpr (stage_lay(LAY) == LAY_FT) {
+      // values pre-offset by the window's integer sample (absolute index lo + k + tau)
+      float2* side = reinterpret_cast<float2*>(bufq + P.cap + kZeroSlots) + si.w;
+      for (int k = lane; k < si.z; k += 32) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (P.storage == STORE_F32) {
+            v[u] = r32[k + u];
+          } else {
+            const uint32_t b = r16[k + u];
+            v[u] = (f16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
+          }
+        }
+        const float it = (float)(si.y + k + P.tau);
+        const float d0 = v[1] - v[0], d1 = v[2] - v[1], d2 = v[3] - v[2];
+        dst[k] = make_float4(fmaf(-it, d0, v[0]), fmaf(-it, d2, v[2]), d0, d2);
+        side[k] = make_float2(fmaf(-it, d1, v[1]), d1);
+      }
+      continue;
+    }
     for (int k = lane; k < si.z; k += 32) {
       float v[4];
 #pragma unroll
@@ -770,6 +802,53 @@ template <int W>
 struct FastAcc<W, LAY_PD> : PDAcc<W, false> {};
 template <int W>
 struct FastAcc<W, LAY_PDS> : PDAcc<W, true> {};
+
+// Pre-offset values (LAY_FT, w = 3): the window at main entry address a and side
+// entry address b, interpolated at traveltime t (samples): v_j = F_j + t d_j.
+template <int W>
+struct FastAcc<W, LAY_FT> {
+  static_assert(W == 3, "the pre-offset layout is for w = 3");
+  float2 np;     // (num_0, num_2)
+  float ns;      // num_1
+  float2 den2;   // energy of the current chunk, two partial sums
+  int M;
+
+  __device__ __forceinline__ void reset() {
+    np = make_float2(0.f, 0.f);
+    ns = 0.f;
+    den2 = make_float2(0.f, 0.f);
+    M = 0;
+  }
+  __device__ __forceinline__ void add_ft(uint32_t a, uint32_t b, float t) {
+    const float4 A = lds128(a);   // (F_0, F_2, d_0, d_2)
+    const float2 B = lds64(b);    // (F_1, d_1)
+    const float2 v = make_float2(fmaf(A.z, t, A.x), fmaf(A.w, t, A.y));
+    const float v1 = fmaf(B.y, t, B.x);
+    np = __fadd2_rn(np, v);
+    den2 = __ffma2_rn(v, v, den2);
+    ns += v1;
+    den2.x = fmaf(v1, v1, den2.x);
+  }
+  // the same sums from window samples sv[0..3] at weight x (a path the variants of
+  // this layout do not take: they stage every window)
+  __device__ __forceinline__ void add_samples(const float* sv, float x) {
+    const float v0 = fmaf(sv[1] - sv[0], x, sv[0]), v1 = fmaf(sv[2] - sv[1], x, sv[1]);
+    const float v2 = fmaf(sv[3] - sv[2], x, sv[2]);
+    np = __fadd2_rn(np, make_float2(v0, v2));
+    den2 = __ffma2_rn(make_float2(v0, v2), make_float2(v0, v2), den2);
+    ns += v1;
+    den2.x = fmaf(v1, v1, den2.x);
+  }
+  __device__ __forceinline__ float take_energy() {
+    const float e = den2.x + den2.y;
+    den2 = make_float2(0.f, 0.f);
+    return e;
+  }
+  __device__ __forceinline__ void sums(float& acsq, float& lin) const {
+    acsq = fmaf(np.x, np.x, fmaf(np.y, np.y, ns * ns));
+    lin = np.x + np.y + ns;
+  }
+};
 
 
 
