@@ -78,7 +78,7 @@ int launch_stt00(int w, int cdp0, int cdp1, const KParams& P, float a, float b, 
 int launch_repick(int w, const RepickParams& R, cudaStream_t st) {
   const int64_t items = R.item_end - R.item0;
   if (items <= 0) return SEMB_OK;
-  const int grid = (int)((items + 7) / 8);
+  const int grid = (int)((items + 255) / 256);   // 32 items per warp, 8 warps per CTA
   switch (w) {
     case 1: k_repick<1><<<grid, 256, 0, st>>>(R); break;
     case 3: k_repick<3><<<grid, 256, 0, st>>>(R); break;

@@ -401,7 +401,39 @@ __device__ bool eval_f64_ordered(const RepickParams& R, int64_t e0, int64_t e1, 
   return false;
 }
 
-// Final pick per (CDP, t0), one warp each.  When the best two FP32 candidates are
+// The outputs of one (CDP, t0) item: the pick (or the no-pick values of the
+// reference: CMP ctr -1, stack 0; CRS ctr 0, the stack of item (t0 = 0, candidate 0))
+// and, when kept, the second-best candidate and the FP64 error of the pick.
+__device__ __forceinline__ void write_pick(const RepickParams& R, int64_t item, int cdp, bool none, int out_i,
+                                           float out_s, float out_k, float err, const float* ts, const int* ti0) {
+  if (R.sem2) {
+    // the best single-precision candidate other than the pick
+    float s2 = 0.f;
+    int i2 = -1;
+    if (!none) {
+#pragma unroll
+      for (int q = kTopK - 1; q >= 0; --q)
+        if (ti0[q] >= 0 && ts[q] > 0.f && ti0[q] != out_i) {
+          s2 = ts[q];
+          i2 = ti0[q];
+        }
+    }
+    R.sem2[item] = s2;
+    R.idx2[item] = i2;
+    R.err64[item] = err;
+  }
+  if (none) {
+    R.ctr[item] = R.method == METHOD_CMP ? -1 : 0;
+    R.str[item] = 0.f;
+    R.stk[item] = R.method == METHOD_CMP ? 0.f : R.stt00[cdp];
+  } else {
+    R.ctr[item] = out_i;
+    R.str[item] = out_s;
+    R.stk[item] = out_k;
+  }
+}
+
+// One near-tie item, all lanes of the warp: when the best two FP32 candidates are
 // closer than the near-tie band (repick_band: `gap`, wider for small apertures), or
 // always in mode 2, the top-4 are re-evaluated in FP64 with the reference's
 // double-precision arithmetic (CRS/OpenMP/src/main.cpp:209-267 with real = double)
@@ -410,10 +442,7 @@ __device__ bool eval_f64_ordered(const RepickParams& R, int64_t e0, int64_t e1, 
 // (eval_f64_ordered, one candidate per lane), so that a candidate the FP32 ranking
 // put fifth or lower can still win as it does in FP64.
 template <int W>
-static __global__ void k_repick(RepickParams R) {
-  const int lane = threadIdx.x & 31;
-  const int64_t item = R.item0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (item >= R.item_end) return;
+__device__ void repick_item(const RepickParams& R, const int64_t item, const int lane) {
   const int cdp = (int)(item / R.ns);
   const int t0 = (int)(item - (int64_t)cdp * R.ns);
   float ts[kTopK], tk[kTopK];
@@ -571,32 +600,42 @@ static __global__ void k_repick(RepickParams R) {
     }
     if (lane == 0) atomicAdd(R.repicked, 1ull);
   }
-  if (R.sem2 && lane == 0) {
-    // the best single-precision candidate other than the pick
-    float s2 = 0.f;
-    int i2 = -1;
-    if (!none) {
+  if (lane == 0) write_pick(R, item, cdp, none, out_i, out_s, out_k, err, ts, ti0);
+}
+
+// Final pick per (CDP, t0), 32 consecutive items per warp: each lane screens one
+// item (no candidate above 0, or no near tie: the FP32 pick stands and the lane writes
+// it), then the warp takes the near-tie items one after the other (repick_item), all
+// lanes on one item's FP64 evaluation.
+template <int W>
+static __global__ void k_repick(RepickParams R) {
+  const int lane = threadIdx.x & 31;
+  const int64_t base = R.item0 + ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+  if (base >= R.item_end) return;
+  const int64_t item = base + lane;
+  bool redo = false;
+  if (item < R.item_end) {
+    const int cdp = (int)(item / R.ns);
+    float ts[kTopK], tk[kTopK];
+    int ti[kTopK];
 #pragma unroll
-      for (int q = kTopK - 1; q >= 0; --q)
-        if (ti0[q] >= 0 && ts[q] > 0.f && ti0[q] != out_i) {
-          s2 = ts[q];
-          i2 = ti0[q];
-        }
+    for (int q = 0; q < kTopK; ++q) {
+      ts[q] = R.top_sem[item * kTopK + q];
+      ti[q] = R.top_idx[item * kTopK + q];
+      tk[q] = R.top_stk[item * kTopK + q];
     }
-    R.sem2[item] = s2;
-    R.idx2[item] = i2;
-    R.err64[item] = err;
+    const int napert = (int)(R.ap_off[cdp + 1] - R.ap_off[cdp]);
+    const float band = repick_band(R.gap, napert);
+    const bool none = !(ts[0] > 0.f) || ti[0] < 0;
+    const bool near_tie = ti[1] >= 0 && ts[1] > 0.f && (ts[0] - ts[1]) < band;
+    redo = !none && (R.mode == 2 || (R.mode == 1 && near_tie));
+    if (!redo) write_pick(R, item, cdp, none, ti[0], ts[0], tk[0], -1.f, ts, ti);
   }
-  if (lane == 0) {
-    if (none) {
-      R.ctr[item] = R.method == METHOD_CMP ? -1 : 0;
-      R.str[item] = 0.f;
-      R.stk[item] = R.method == METHOD_CMP ? 0.f : R.stt00[cdp];
-    } else {
-      R.ctr[item] = out_i;
-      R.str[item] = out_s;
-      R.stk[item] = out_k;
-    }
+  unsigned todo = __ballot_sync(0xffffffffu, redo);
+  while (todo) {
+    const int src = __ffs(todo) - 1;
+    todo &= todo - 1;
+    repick_item<W>(R, base + src, lane);
   }
 }
 
