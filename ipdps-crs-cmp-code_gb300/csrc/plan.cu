@@ -100,6 +100,7 @@ struct semb_plan {
 
   // device buffers
   float* d_samples = nullptr;
+  float* d_ingest = nullptr;   // staging of the linear trace copies (copy_traces)
   uint16_t* d_samples16 = nullptr;
   float* d_scale = nullptr;
   int64_t* d_ap_off = nullptr;
@@ -236,6 +237,7 @@ void free_data(semb_plan* pl, bool keep_reusable = false) {
     dev_free(ptr);
   };
   release(pl->d_samples);
+  release(pl->d_ingest);
   release(pl->d_samples16);
   release(pl->d_scale);
   release(pl->d_ap_off);
@@ -618,19 +620,27 @@ int semb_plan_stream(semb_plan* pl, const semb_gather_view* g, int32_t nchunks) 
 
 namespace {
 
-// Traces [t0, t1) of the gather into the device stores on stream cs: the pitched
-// FP32 rows with their zero padding (one 2-D copy) and, batched, the 16-bit rows.
+// Traces [t0, t1) of the gather into the device stores on stream cs: linear copies of
+// up to kIngestBytes of the caller's trace-major samples into a staging buffer (the
+// copy engine's fastest form), each followed by k_ingest_rows, which lays the rows out
+// at the plan's pitch with their zero padding and builds the 16-bit batched store.
+constexpr int64_t kIngestBytes = (int64_t)1 << 30;
+
 int copy_traces(semb_plan* pl, const semb_gather_view* g, int64_t t0, int64_t t1, cudaStream_t cs) {
   const int64_t n = t1 - t0;
   if (n <= 0) return SEMB_OK;
-  float* dst = pl->d_samples + t0 * pl->pitch;
-  SEMB_CUDA(cudaMemsetAsync(dst, 0, (size_t)n * pl->pitch * sizeof(float), cs));
-  SEMB_CUDA(cudaMemcpy2DAsync(dst, pl->pitch * sizeof(float), g->samples + t0 * g->ns, (size_t)g->ns * sizeof(float),
-                              (size_t)g->ns * sizeof(float), (size_t)n, cudaMemcpyHostToDevice, cs));
-  if (pl->p.mode == SEMB_BATCHED && pl->p.storage != SEMB_STORE_F32) {
-    k_make_store16<<<(int)std::min<int64_t>(n, 65535), 256, 0, cs>>>(n, g->ns, pl->pitch, pl->p.storage, dst,
-                                                                     pl->d_samples16 + t0 * pl->pitch,
-                                                                     pl->d_scale + t0);
+  const int64_t row_bytes = (int64_t)g->ns * (int64_t)sizeof(float);
+  const int64_t per = std::max<int64_t>(1, kIngestBytes / row_bytes);
+  // one size for every call of an upload (the streamed run copies chunk after chunk)
+  SEMB_TRY(dev_reuse(pl, &pl->d_ingest, (size_t)std::min(pl->ntraces, per) * g->ns));
+  const bool s16 = pl->p.mode == SEMB_BATCHED && pl->p.storage != SEMB_STORE_F32;
+  for (int64_t r0 = t0; r0 < t1; r0 += per) {
+    const int64_t r1 = std::min(t1, r0 + per);
+    SEMB_CUDA(cudaMemcpyAsync(pl->d_ingest, g->samples + r0 * g->ns, (size_t)((r1 - r0) * row_bytes),
+                              cudaMemcpyHostToDevice, cs));
+    k_ingest_rows<<<(int)std::min<int64_t>(r1 - r0, 65535), 256, 0, cs>>>(
+        r1 - r0, g->ns, pl->pitch, pl->p.storage, pl->d_ingest, pl->d_samples + r0 * pl->pitch,
+        s16 ? pl->d_samples16 + r0 * pl->pitch : nullptr, s16 ? pl->d_scale + r0 : nullptr);
     SEMB_CUDA(cudaGetLastError());
   }
   return SEMB_OK;

@@ -206,33 +206,43 @@ static __global__ void k_aperture_fill(int ncdps, int method, const int64_t* __r
   }
 }
 
-// 16-bit trace store: per trace, scale = max|s| / 32768 (1 for an all-zero trace)
-// and s16 = s / scale rounded to nearest.  One block per trace.
-static __global__ void k_make_store16(int64_t ntr, int ns, int64_t pitch, int storage, const float* __restrict__ s32,
-                               uint16_t* __restrict__ s16, float* __restrict__ scale) {
+// Traces copied linearly (ns samples each, back to back, as the caller holds them)
+// into the device stores: the FP32 rows at the plan's pitch with their zero padding
+// and, for a 16-bit batched store (s16 not null), the FP16/BF16 rows of the samples
+// divided by the per-trace scale max|s| / 32768 (1 for an all-zero or non-finite
+// trace), with the same padding.  One CTA per trace, grid-stride over traces.
+static __global__ void k_ingest_rows(int64_t ntr, int ns, int64_t pitch, int storage, const float* __restrict__ src,
+                                     float* __restrict__ s32, uint16_t* __restrict__ s16, float* __restrict__ scale) {
   __shared__ float red[32];
   for (int64_t tr = blockIdx.x; tr < ntr; tr += gridDim.x) {
-    const float* row = s32 + tr * pitch;
-    float m = 0.f;
-    for (int k = threadIdx.x; k < ns; k += blockDim.x) m = fmaxf(m, fabsf(row[k]));
+    const float* row = src + tr * ns;
+    float sc = 1.0f;
+    if (s16) {
+      float m = 0.f;
+      for (int k = threadIdx.x; k < ns; k += blockDim.x) m = fmaxf(m, fabsf(row[k]));
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+      for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-      if (threadIdx.x == 0) red[0] = v;
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) red[0] = v;
+      }
+      __syncthreads();
+      const float mx = red[0];
+      sc = (mx > 0.f && isfinite(mx)) ? mx / 32768.0f : 1.0f;
+      if (threadIdx.x == 0) scale[tr] = sc;
     }
-    __syncthreads();
-    const float mx = red[0];
-    const float sc = (mx > 0.f && isfinite(mx)) ? mx / 32768.0f : 1.0f;
-    if (threadIdx.x == 0) scale[tr] = sc;
     for (int k = threadIdx.x; k < pitch; k += blockDim.x) {
-      const float v = k < ns ? row[k] / sc : 0.f;
-      s16[tr * pitch + k] = storage == STORE_BF16 ? __bfloat16_as_ushort(__float2bfloat16_rn(v))
-                                                  : __half_as_ushort(__float2half_rn(v));
+      const float v = k < ns ? row[k] : 0.f;
+      s32[tr * pitch + k] = v;
+      if (s16) {
+        const float q = v / sc;
+        s16[tr * pitch + k] = storage == STORE_BF16 ? __bfloat16_as_ushort(__float2bfloat16_rn(q))
+                                                    : __half_as_ushort(__float2half_rn(q));
+      }
     }
     __syncthreads();
   }
