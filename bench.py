@@ -358,6 +358,8 @@ def errors_vs_fp64(oracle, s, method, cdp_end, outs: dict, idx, t0_blocks=None, 
         same = c == ref["ctr"]
         res[name] = {"sem_max_abs": float(np.max(np.abs(sm - ref["str"]))),
                      "stack_max_abs": float(np.max(np.abs(sk - ref["stk"]))),
+                     # a differing pick stacks along another candidate's traveltime
+                     "stack_max_abs_same_pick": float(np.max(np.abs(sk - ref["stk"])[same])) if same.any() else None,
                      "identical_picks": float(same.mean()),
                      "identical_picks_decisive": float(same[decisive].mean()) if decisive.any() else None}
     return res
@@ -563,6 +565,7 @@ def run_chunked_survey(args):
                 "pairs": int(same.size), "decisive_pairs": int(decisive.sum()),
                 "sem_max_abs": float(np.max(np.abs(sm - ref["str"]))),
                 "stack_max_abs": float(np.max(np.abs(sk - ref["stk"]))),
+                "stack_max_abs_same_pick": float(np.max(np.abs(sk - ref["stk"])[same])) if same.any() else None,
                 "identical_picks": float(same.mean()),
                 "identical_picks_decisive": float(same[decisive].mean()) if decisive.any() else None}
             os.unlink(err_path)

@@ -38,7 +38,7 @@ extern "C" {
 #define SEMB_ABI_VERSION 8
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
-#define SEMB_MAX_VARIANTS 24
+#define SEMB_MAX_VARIANTS 32
 
 /* Aperture buckets of a batched plan's work queue (semb_plan_buckets). */
 #define SEMB_MAX_BUCKETS 4

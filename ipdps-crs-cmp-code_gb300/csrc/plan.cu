@@ -417,7 +417,7 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   int cap = form == FORM_PLAIN ? 32768 : 8192;
   if (form == FORM_FAST && pl->stage_cap > 0) cap = std::min(cap, pl->stage_cap);
   auto smem_of = [&](int cp) {
-    return pipe ? pipe_layout(rc, cp, store, nt, lay).total : smem_layout(form, rc, cp, store, nt).total;
+    return pipe ? pipe_layout(rc, cp, store, nt, lay).total : smem_layout(form, rc, cp, store, nt, lay).total;
   };
   while (cap > 64 && smem_of(cap) > budget) cap -= 64;
   int min_cap = (int)pl->pitch + 16;

@@ -10,9 +10,11 @@
 // layout (LAY_SD) saves one FP32 op per window sample for 50% more shared-memory
 // bytes per evaluation; the packed layout (LAY_P2) does two window samples per
 // FP32x2 instruction, and LAY_PD (w = 3) stores the pair's differences in place of
-// the odd samples (its variant unrolls the in-range trace loop by two).  Variants 11 and up use the pipelined kernel
-// (semb_pipe_kernel), whose warps hand chunks over through mbarriers instead of
-// meeting at CTA barriers.  RC values keep the per-item
+// the odd samples (its variant unrolls the in-range trace loop by two); LAY_PD5
+// (w = 5) adds an 8-byte side entry per sample.  pipe_entry variants use the pipelined
+// kernel (semb_pipe_kernel), whose warps hand chunks over through mbarriers instead of
+// meeting at CTA barriers; xp_entry variants are the two-barrier kernel with the first
+// chunk of each pass staged ahead.  RC values keep the per-item
 // register state within 65536 / (256 * MINB) registers without spilling
 // (checked with -Xptxas -v).
 #pragma once
@@ -37,10 +39,16 @@ struct SearchEntry {
 constexpr int kMaxVariants = SEMB_MAX_VARIANTS;
 
 template <int METHOD, int FORM, int W, int RC, int MINB, int LAY = LAY_QUAD, bool BRUN = false, int NT = 256,
-          bool GLOB = false>
+          bool GLOB = false, bool XP = false>
 SearchEntry entry() {
-  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT, GLOB>, RC, MINB, BRUN ? 1 : 0, NT,
-          0, LAY, GLOB ? 1 : 0};
+  return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT, GLOB, XP>, RC, MINB, BRUN ? 1 : 0,
+          NT, 0, LAY, GLOB ? 1 : 0};
+}
+
+// the two-barrier batched kernel with its chunk stream run on across passes and tasks
+template <int METHOD, int FORM, int W, int RC, int MINB, int LAY>
+SearchEntry xp_entry() {
+  return entry<METHOD, FORM, W, RC, MINB, LAY, false, 256, false, true>();
 }
 
 template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256, int TU = 1,
@@ -116,6 +124,9 @@ SearchEntry search_entry(int w, int variant) {
       // pre-offset values: no per-item interpolation weight (24 staged bytes per sample)
       if (variant == 22) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_FT, METHOD == METHOD_CRS, 512, 2>();
       if (variant == 23) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_FT, METHOD == METHOD_CRS, 512>();
+      // variants 8 and 21 with the first chunk of each pass staged ahead (XP)
+      if (variant == 24) return xp_entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2>();
+      if (variant == 25) return xp_entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2S>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -140,6 +151,13 @@ SearchEntry search_entry(int w, int variant) {
       if (variant == 19) return pipe_entry<METHOD, 5, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_P2S, METHOD == METHOD_CRS, 512>();
       if (variant == 20) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 7), 4, LAY_P2S, METHOD == METHOD_CRS, 128>();
       if (variant == 21) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2S>();
+      // packed value/difference entries with side entries: 24 staged bytes per item
+      if (variant == 22) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_PD5>();
+      if (variant == 23) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_PD5S>();
+      // variants 21, 22 and 23 with the first chunk of each pass staged ahead (XP)
+      if (variant == 24) return xp_entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2S>();
+      if (variant == 25) return xp_entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_PD5>();
+      if (variant == 26) return xp_entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_PD5S>();
       break;
 #if SEMB_WIDE_WINDOWS
     case 7: if (variant == 0) return entry<METHOD, FORM, 7, 4, 2>(); break;

@@ -220,16 +220,30 @@ constexpr int LAY_PDS = 5;
 // ns <= 8192 only.
 constexpr int LAY_FT = 6;
 constexpr int kMaxNsFT = 8192;
+// w = 5: the packed value/difference entry (s_k, s_k+2, d_k, d_k+2) of LAY_PD and an
+// 8-byte side entry (s_k, d_k) per sample, d_m = s_m+1 - s_m.  An item whose window
+// starts at k reads entry k and side entry k+4: 24 bytes, i.e. six shared-memory
+// wavefronts per warp instead of the eight of two 16-byte entries (LAY_P2), and
+// the pairs (0, 2) and (1, 3) need no differences formed from two loaded values
+// but (s_2, s_4) - (s_1, s_3).  LAY_PD5S forms the interpolated pairs with scalar
+// FMAs (no (x, x) operand).
+constexpr int LAY_PD5 = 7;
+constexpr int LAY_PD5S = 8;
 
 // layout of the staged entries of an accumulation layout
 __host__ __device__ constexpr int stage_lay(int lay) {
-  return lay == LAY_P2S ? LAY_P2 : lay == LAY_PDS ? LAY_PD : lay;
+  return lay == LAY_P2S ? LAY_P2 : lay == LAY_PDS ? LAY_PD : lay == LAY_PD5S ? LAY_PD5 : lay;
+}
+
+// layouts with an 8-byte side entry per sample after the main entries
+__host__ __device__ constexpr bool lay_has_side(int lay) {
+  return stage_lay(lay) == LAY_FT || stage_lay(lay) == LAY_PD5;
 }
 
 // bytes of one staged entry (the address stride of an item's window), and of one
-// staged sample with its side entry (LAY_FT)
+// staged sample with its side entry (LAY_FT, LAY_PD5)
 __host__ __device__ constexpr int lay_entry_bytes(int) { return 16; }
-__host__ __device__ constexpr int lay_stage_bytes(int lay) { return lay == LAY_FT ? 24 : 16; }
+__host__ __device__ constexpr int lay_stage_bytes(int lay) { return lay_has_side(lay) ? 24 : 16; }
 
 struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
@@ -260,7 +274,9 @@ __device__ __forceinline__ int entry_slot(const ChunkMeta* m, int i) {
 //   top-K     per-thread running picks [3][K][nt]
 //   kahan     fast form: per-item compensated energy totals [2][RC][nt]
 //   buf       staging buffer: cap floats (plain) or cap 16-byte quads (fast),
-//             followed by kZeroSlots zeroed slots read by out-of-range items
+//             followed by kZeroSlots zeroed slots read by out-of-range items;
+//             layouts with side entries (LAY_PD5) then hold cap + kZeroSlots
+//             8-byte side entries, the last kZeroSlots zeroed
 //   raw[2]    fast form: the raw windows of two chunks as stored in HBM
 //             (16-bit or FP32), cap + 8*kMaxChunk samples each
 struct SmemLayout {
@@ -269,7 +285,7 @@ struct SmemLayout {
 
 __host__ __device__ inline size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
 
-__host__ __device__ inline SmemLayout smem_layout(int form, int rc, int cap, int storage, int nt) {
+__host__ __device__ inline SmemLayout smem_layout(int form, int rc, int cap, int storage, int nt, int lay) {
   const int K = form == 1 ? 4 : 1;
   SmemLayout L;
   L.meta = 64;
@@ -277,7 +293,7 @@ __host__ __device__ inline SmemLayout smem_layout(int form, int rc, int cap, int
   L.tops = L.src + 2 * kMaxChunk * sizeof(int4);
   L.kahan = L.tops + align128(3 * (size_t)K * nt * 4);
   L.buf = L.kahan + (form == 1 ? 2 * (size_t)rc * nt * 4 : 0);
-  const size_t unit = form == 1 ? 16 : 4;
+  const size_t unit = form == 1 ? (size_t)lay_stage_bytes(lay) : 4;
   const size_t raw_end = L.buf + align128(((size_t)cap + kZeroSlots) * unit);
   if (form == 1) {
     const size_t rb = align128(((size_t)cap + 8 * kMaxChunk) * (storage == 0 ? 4 : 2));
@@ -526,8 +542,12 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
       constexpr int SL = stage_lay(LAY);
       dst[k] = SL == LAY_SD   ? make_float4(v[0], v[1] - v[0], v[1], v[2] - v[1])
                : SL == LAY_P2 ? make_float4(v[0], v[2], v[1], v[3])
-               : SL == LAY_PD ? make_float4(v[0], v[2], v[1] - v[0], v[3] - v[2])
-                               : make_float4(v[0], v[1], v[2], v[3]);
+               : (SL == LAY_PD || SL == LAY_PD5) ? make_float4(v[0], v[2], v[1] - v[0], v[3] - v[2])
+                                                 : make_float4(v[0], v[1], v[2], v[3]);
+      if constexpr (SL == LAY_PD5) {
+        // side entry (s_k, d_k), after the main entries and their zero block
+        reinterpret_cast<float2*>(bufq + P.cap + kZeroSlots)[si.w + k] = make_float2(v[0], v[1] - v[0]);
+      }
     }
   }
 }
@@ -803,6 +823,61 @@ struct FastAcc<W, LAY_PD> : PDAcc<W, false> {};
 template <int W>
 struct FastAcc<W, LAY_PDS> : PDAcc<W, true> {};
 
+// w = 5 with side entries (LAY_PD5): the window at main entry address a, A = (s_0,
+// s_2, d_0, d_2), and side entry address b of entry k+4, B = (s_4, d_4).  Window
+// samples (0, 2) interpolate straight from A; (s_1, s_3) = (s_0, s_2) + (d_0, d_2)
+// (within a rounding of the stored values), (d_1, d_3) = (s_2 - s_1, s_4 - s_3);
+// sample 4 from B.
+template <int W, bool SV>
+struct PD5Acc {
+  static_assert(W == 5, "the side-entry layout is for w = 5");
+  float2 np02, np13;   // (num_0, num_2), (num_1, num_3)
+  float ns;            // num_4
+  float2 den2;         // energy of the current chunk, two partial sums
+  int M;
+
+  __device__ __forceinline__ void reset() {
+    np02 = np13 = make_float2(0.f, 0.f);
+    ns = 0.f;
+    den2 = make_float2(0.f, 0.f);
+    M = 0;
+  }
+  __device__ __forceinline__ void add_side(uint32_t a, uint32_t b, float x) { acc(lds128(a), lds64(b), x); }
+  // the same sums from window samples sv[0..5] of the FP32 store
+  __device__ __forceinline__ void add_samples(const float* sv, float x) {
+    acc(make_float4(sv[0], sv[2], sv[1] - sv[0], sv[3] - sv[2]), make_float2(sv[4], sv[5] - sv[4]), x);
+  }
+  __device__ __forceinline__ void acc(const float4 A, const float2 B, float x) {
+    const float2 v02 = SV ? make_float2(fmaf(A.z, x, A.x), fmaf(A.w, x, A.y))
+                          : __ffma2_rn(make_float2(A.z, A.w), make_float2(x, x), make_float2(A.x, A.y));
+    const float2 s13 = __fadd2_rn(make_float2(A.x, A.y), make_float2(A.z, A.w));
+    const float2 d13 = make_float2(A.y - s13.x, B.x - s13.y);
+    const float2 v13 = SV ? make_float2(fmaf(d13.x, x, s13.x), fmaf(d13.y, x, s13.y))
+                          : __ffma2_rn(d13, make_float2(x, x), s13);
+    const float v4 = fmaf(B.y, x, B.x);
+    np02 = __fadd2_rn(np02, v02);
+    np13 = __fadd2_rn(np13, v13);
+    ns += v4;
+    den2 = __ffma2_rn(v02, v02, den2);
+    den2 = __ffma2_rn(v13, v13, den2);
+    den2.x = fmaf(v4, v4, den2.x);
+  }
+  __device__ __forceinline__ float take_energy() {
+    const float e = den2.x + den2.y;
+    den2 = make_float2(0.f, 0.f);
+    return e;
+  }
+  __device__ __forceinline__ void sums(float& acsq, float& lin) const {
+    acsq = fmaf(np02.x, np02.x, fmaf(np02.y, np02.y, fmaf(np13.x, np13.x, fmaf(np13.y, np13.y, ns * ns))));
+    lin = np02.x + np02.y + np13.x + np13.y + ns;
+  }
+};
+
+template <int W>
+struct FastAcc<W, LAY_PD5> : PD5Acc<W, false> {};
+template <int W>
+struct FastAcc<W, LAY_PD5S> : PD5Acc<W, true> {};
+
 // Pre-offset values (LAY_FT, w = 3): the window at main entry address a and side
 // entry address b, interpolated at traveltime t (samples): v_j = F_j + t d_j.
 template <int W>
@@ -895,10 +970,16 @@ __device__ __forceinline__ void global_entry(const KParams& P, int tr, float4 g,
 // buffer are read from the FP32 store (kGlobalEntry).  Without it the plan gives
 // the variant a buffer that holds any window, and the path is not compiled (it
 // costs registers in the partly-in-range loop).
-template <int METHOD, int FORM, int W, int RC, int MINB, int LAY, bool BRUN, int NT, bool GLOB = false>
+// XP (batched form): the chunk stream runs on across passes and tasks.  While the
+// warps compute the last chunk of a pass, warp 0 plans the first chunk of the next
+// pass, or, after the last pass, takes the next task from the queue and plans its
+// first chunk, so that its copies land during that computation; without XP every
+// pass starts by planning its first chunk and waiting for its copies.
+template <int METHOD, int FORM, int W, int RC, int MINB, int LAY, bool BRUN, int NT, bool GLOB = false,
+          bool XP = false>
 __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage, NT);
+  const SmemLayout L = smem_layout(FORM, RC, P.cap, P.storage, NT, LAY);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);   // [2]
   int* ctl = reinterpret_cast<int*>(smem_raw + 16);
   ChunkMeta* metas = reinterpret_cast<ChunkMeta*>(smem_raw + L.meta);   // [2], stride kMetaBytes
@@ -929,6 +1010,8 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
     if (threadIdx.x < kZeroSlots) buf[P.cap + threadIdx.x] = 0.f;
   } else {
     if (threadIdx.x < kZeroSlots) bufq[P.cap + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lay_has_side(LAY) && threadIdx.x < kZeroSlots)   // the side entries' zero block
+      reinterpret_cast<float2*>(bufq + P.cap + kZeroSlots)[P.cap + threadIdx.x] = make_float2(0.f, 0.f);
   }
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
@@ -940,15 +1023,24 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
   uint32_t phases = 0;   // fast form: bit i = parity of bars[i]
 
   int task_iter = 0;
+  // XP: the staging state carried from one pass (or task) to the next
+  int cur = 0;             // buffer (meta, raw, barrier) of the next chunk
+  bool pre = false;        // its first chunk is planned in buffer cur, copies issued
+  bool task_pre = false;   // the next task was taken from the queue (ctl[0]); ctl[1]
+                           // says whether its first chunk is planned
   for (;;) {
     int task;
     if (FORM == FORM_PLAIN) {
       if (task_iter > 0) break;
       task = blockIdx.x;
     } else {
-      if (threadIdx.x == 0) ctl[0] = atomicAdd(P.counter, 1);
-      __syncthreads();
+      if (!(XP && task_pre)) {
+        if (threadIdx.x == 0) ctl[0] = atomicAdd(P.counter, 1);
+        __syncthreads();
+      }
       task = ctl[0];
+      pre = XP && task_pre && ctl[1] != 0;
+      task_pre = false;
       __syncthreads();
     }
     ++task_iter;
@@ -1073,6 +1165,10 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
         } else {
           const int n_in = meta->n_in;
           const uint32_t top = bufq_addr + 16u * (uint32_t)P.cap;
+          // side entries (LAY_PD5): the side entry of window sample W-1 of the item
+          // at main entry address a is at a / 2 + side_shift
+          const uint32_t side_shift =
+              bufq_addr + 16u * (uint32_t)(P.cap + kZeroSlots) + 8u * (uint32_t)(W - 1) - (bufq_addr >> 1);
           // traces on which every item is in range: traveltimes of item pairs in
           // FP32x2, address = bits(t + 2^23) * 16 + base (mod 2^32), clamped to the
           // buffer as a guard
@@ -1106,8 +1202,17 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
                 report_window(P.status, __float_as_int(y.x) + i0, W, srcc[e], cdp, t0);
                 if (2 * rp + 1 < RC) report_window(P.status, __float_as_int(y.y) + i0, W, srcc[e], cdp, t0);
               }
-              fa[2 * rp].add(min(__float_as_uint(y.x) * 16u + base, top), x.x);
-              if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * 16u + base, top), x.y);
+              if constexpr (lay_has_side(LAY)) {
+                const uint32_t a0 = min(__float_as_uint(y.x) * 16u + base, top);
+                fa[2 * rp].add_side(a0, (a0 >> 1) + side_shift, x.x);
+                if (2 * rp + 1 < RC) {
+                  const uint32_t a1 = min(__float_as_uint(y.y) * 16u + base, top);
+                  fa[2 * rp + 1].add_side(a1, (a1 >> 1) + side_shift, x.y);
+                }
+              } else {
+                fa[2 * rp].add(min(__float_as_uint(y.x) * 16u + base, top), x.x);
+                if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * 16u + base, top), x.y);
+              }
             }
           }
           // the other traces: per-item range checks; an out-of-range item reads the
@@ -1144,7 +1249,12 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
               if constexpr (SEMB_CHECKED) {
                 if (ok) report_window(P.status, soff + rel, W, srcc[e], cdp, t0);
               }
-              fa[r].add(bufq_addr + 16u * idx, x);
+              if constexpr (lay_has_side(LAY)) {
+                const uint32_t a = bufq_addr + 16u * idx;
+                fa[r].add_side(a, (a >> 1) + side_shift, x);
+              } else {
+                fa[r].add(bufq_addr + 16u * idx, x);
+              }
               fa[r].M += ok ? 1 : 0;
             }
           }
@@ -1187,12 +1297,15 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
       } else {
         // software pipeline: while all warps compute chunk c from the quad buffer,
         // the raw windows of chunk c+1 land in the other raw buffer by TMA
-        int cur = 0;
-        if (warp == 0) {
-          plan_chunk<METHOD, FORM>(P, pb, ap_begin, ap_end, T_lo, T_hi, meta_at(0), srcs);
-          issue_raw(P, meta_at(0), srcs, raw_at(0), &bars[0]);
+        if (!XP) cur = 0;
+        if (!pre && ap_begin < ap_end) {
+          if (warp == 0) {
+            plan_chunk<METHOD, FORM>(P, pb, ap_begin, ap_end, T_lo, T_hi, meta_at(cur), srcs + cur * kMaxChunk);
+            issue_raw(P, meta_at(cur), srcs + cur * kMaxChunk, raw_at(cur), bars + cur);
+          }
+          __syncthreads();
         }
-        __syncthreads();
+        pre = false;
         int64_t ap_pos = ap_begin;
         while (ap_pos < ap_end) {
           ChunkMeta* mc = meta_at(cur);
@@ -1207,17 +1320,47 @@ __global__ void __launch_bounds__(NT, MINB) semb_search_kernel(KParams P) {
             return;
           }
           const int64_t next = ap_pos + mc->consumed;
+          const bool last_pass = pass + 1 == P.npass;
           if (warp == 0) {
             ChunkMeta* mn = meta_at(cur ^ 1);
+            int4* sn = srcs + (cur ^ 1) * kMaxChunk;
             if (next < ap_end) {
-              plan_chunk<METHOD, FORM>(P, pb, next, ap_end, T_lo, T_hi, mn, srcs + (cur ^ 1) * kMaxChunk);
-              issue_raw(P, mn, srcs + (cur ^ 1) * kMaxChunk, raw_at(cur ^ 1), bars + (cur ^ 1));
+              plan_chunk<METHOD, FORM>(P, pb, next, ap_end, T_lo, T_hi, mn, sn);
+              issue_raw(P, mn, sn, raw_at(cur ^ 1), bars + (cur ^ 1));
+            } else if (XP && !last_pass) {
+              // the first chunk of the next pass of this task
+              plan_chunk<METHOD, FORM>(P, pb + 8, ap_begin, ap_end, T_lo, T_hi, mn, sn);
+              issue_raw(P, mn, sn, raw_at(cur ^ 1), bars + (cur ^ 1));
+            } else if (XP) {
+              // the next task and, if it has aperture traces, its first chunk
+              int tn = 0;
+              if (lane == 0) tn = atomicAdd(P.counter, 1);
+              tn = __shfl_sync(0xffffffffu, tn, 0);
+              int planned = 0;
+              if (tn < P.ntasks) {
+                const int2 tdn = P.tasks[tn];
+                const int64_t b = P.ap_off[tdn.x], e = P.ap_off[tdn.x + 1];
+                if (b < e) {
+                  const float tl = P.dt * (float)tdn.y, th = P.dt * (float)min(tdn.y + kTB - 1, P.ns - 1);
+                  plan_chunk<METHOD, FORM>(P, P.pass_bounds, b, e, tl, th, mn, sn);
+                  issue_raw(P, mn, sn, raw_at(cur ^ 1), bars + (cur ^ 1));
+                  planned = 1;
+                }
+              }
+              if (lane == 0) {
+                ctl[0] = tn;
+                ctl[1] = planned;
+              }
             }
           }
           compute_chunk(mc, n, srcs + cur * kMaxChunk);
           __syncthreads();   // quad buffer free; the next chunk's metadata visible
           ap_pos = next;
           cur ^= 1;
+          if (XP && next >= ap_end) {
+            pre = !last_pass;
+            task_pre = last_pass;
+          }
         }
       }
 

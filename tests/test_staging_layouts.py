@@ -31,3 +31,27 @@ def test_packed_value_difference_window_is_the_interpolation():
     ulp = mag * 2.0 ** -23
     for got, want in zip((v0, v1, v2), exact):
         assert np.all(np.abs(got.astype(np.float64) - want) <= 4 * ulp)
+
+
+def test_side_entry_window_w5_is_the_interpolation():
+    """w = 5 with side entries (LAY_PD5): main entry (s_0, s_2, d_0, d_2), side entry
+    (s_4, d_4); (s_1, s_3) = (s_0, s_2) + (d_0, d_2), (d_1, d_3) = (s_2 - s_1, s_4 - s_3).
+    The five window values stay within a few float roundings of the interpolation."""
+    rng = np.random.default_rng(6)
+    n = 200000
+    scale = F(0.61)
+    s = (rng.standard_normal((n, 6)) * 3000).astype(np.float16).astype(F) * scale
+    x = rng.random(n).astype(F)
+    d = [(s[:, j + 1] - s[:, j]).astype(F) for j in range(5)]
+    v0 = fma32(d[0], x, s[:, 0])
+    v2 = fma32(d[2], x, s[:, 2])
+    s1 = (s[:, 0] + d[0]).astype(F)
+    s3 = (s[:, 2] + d[2]).astype(F)
+    v1 = fma32((s[:, 2] - s1).astype(F), x, s1)
+    v3 = fma32((s[:, 4] - s3).astype(F), x, s3)
+    v4 = fma32(d[4], x, s[:, 4])
+    exact = [s[:, j].astype(np.float64) + x.astype(np.float64) * (s[:, j + 1].astype(np.float64) - s[:, j])
+             for j in range(5)]
+    ulp = np.abs(s).max(axis=1).astype(np.float64) * 2.0 ** -23
+    for got, want in zip((v0, v1, v2, v3, v4), exact):
+        assert np.all(np.abs(got.astype(np.float64) - want) <= 4 * ulp)
