@@ -80,7 +80,9 @@ __host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, 
   L.tops = L.src + (size_t)kMetaRing * kMaxChunk * 16;
   L.kahan = L.tops + align128(3 * (size_t)kTopK * nt * 4);
   L.quad = L.kahan + align128(2 * (size_t)rc * nt * 4);
-  L.quad_stride = align128(((size_t)cap + kZeroSlots) * lay_stage_bytes(lay));
+  // LAY_X3: a sample plane and a difference plane of kXPlane floats each (the plan
+  // keeps cap + kZeroSlots within a plane)
+  L.quad_stride = lay == LAY_X3 ? (size_t)8 * kXPlane : align128(((size_t)cap + kZeroSlots) * lay_stage_bytes(lay));
   L.raw = L.quad + kStages * L.quad_stride;
   L.raw_stride = align128(((size_t)cap + 8 * kMaxChunk) * (storage == STORE_F32 ? 4 : 2));
   L.total = L.raw + kRawBufs * L.raw_stride;
@@ -129,6 +131,10 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   for (int s = 0; s < kStages; ++s) {
     if (threadIdx.x < kZeroSlots * (EB / 16))
       quad_at(s)[P.cap * (EB / 16) + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (LAY == LAY_X3 && threadIdx.x < kZeroSlots) {   // both planes' zero blocks
+      reinterpret_cast<float*>(quad_at(s))[P.cap + threadIdx.x] = 0.f;
+      reinterpret_cast<float*>(quad_at(s))[kXPlane + P.cap + threadIdx.x] = 0.f;
+    }
     if (LAY == LAY_FT && threadIdx.x < kZeroSlots)   // the side entries' zero block
       reinterpret_cast<float2*>(quad_at(s) + P.cap + kZeroSlots)[P.cap + threadIdx.x] = make_float2(0.f, 0.f);
   }
@@ -255,7 +261,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   auto CA = [&](int r) { return (r & 1) ? ca2[r >> 1].y : ca2[r >> 1].x; };
   auto CB = [&](int r) { return (r & 1) ? cb2[r >> 1].y : cb2[r >> 1].x; };
   auto CC = [&](int r) { return (r & 1) ? cc2[r >> 1].y : cc2[r >> 1].x; };
-  FastAcc<W, LAY> fa[RC];
+  AccSet<W, LAY, RC> fa;
   int ntask = 0;
   float last_s = 0.f;
   int last_i = 0x7fffffff;
@@ -358,6 +364,14 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
               const uint32_t a1 = min(__float_as_uint(y.y) * EB + base, top);
               fa[2 * rp + 1].add_ft(a1, (a1 >> 1) + side_shift, t.y);
             }
+          } else if constexpr (LAY == LAY_X3) {
+            // both items of the pair in one set of FP32x2 operations
+            const uint32_t a0 = min(__float_as_uint(y.x) * EB + base, top);
+            if (2 * rp + 1 < RC) {
+              fa.add_pair(rp, a0, min(__float_as_uint(y.y) * EB + base, top), x);
+            } else {
+              fa[2 * rp].add(a0, x.x);
+            }
           } else {
             fa[2 * rp].add(min(__float_as_uint(y.x) * EB + base, top), x.x);
             if (2 * rp + 1 < RC) fa[2 * rp + 1].add(min(__float_as_uint(y.y) * EB + base, top), x.y);
@@ -376,7 +390,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
         }
         if (GLOB && soff == kGlobalEntry) {
           // a window larger than a stage: the items read the FP32 store
-          global_entry<METHOD, BRUN>(P, meta->raw[e], g, q0, Tsmp, T2smp, span, ca2, cb2, cc2, fa);
+          if constexpr (GLOB) global_entry<METHOD, BRUN>(P, meta->raw[e], g, q0, Tsmp, T2smp, span, ca2, cb2, cc2, fa.a);
           continue;
         }
 #pragma unroll

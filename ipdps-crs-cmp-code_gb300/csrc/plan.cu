@@ -371,6 +371,10 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
   if (lay == LAY_FT && pl->ns > kMaxNsFT)
     return fail(SEMB_E_ARG, "variant %d (pre-offset values) is for ns <= %d", v, kMaxNsFT);
+  // LAY_X3 stages fixed planes: a whole trace and the zero block must fit one plane
+  if (lay == LAY_X3 && (int64_t)pl->pitch + 16 > kXPlane - kZeroSlots)
+    return fail(SEMB_E_ARG, "variant %d (sample and difference planes) is for ns <= %d", v,
+                kXPlane - kZeroSlots - 24);
   const int ncand = pl->ncand;
   // search order; a negative slot -1-g marks padding that repeats candidate g.
   // B-run variants pad each (A, C) group's run of nb B values to a multiple of RC
@@ -419,6 +423,7 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   auto smem_of = [&](int cp) {
     return pipe ? pipe_layout(rc, cp, store, nt, lay).total : smem_layout(form, rc, cp, store, nt, lay).total;
   };
+  if (lay == LAY_X3) cap = std::min(cap, kXPlane - kZeroSlots);
   while (cap > 64 && smem_of(cap) > budget) cap -= 64;
   int min_cap = (int)pl->pitch + 16;
   if (small_stages) min_cap = std::min(min_cap, pl->stage_cap > 0 ? pl->stage_cap : kMinStage);

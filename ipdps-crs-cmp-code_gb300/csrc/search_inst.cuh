@@ -127,6 +127,9 @@ SearchEntry search_entry(int w, int variant) {
       // variants 8 and 21 with the first chunk of each pass staged ahead (XP)
       if (variant == 24) return xp_entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2>();
       if (variant == 25) return xp_entry<METHOD, FORM, 3, (METHOD == METHOD_CMP ? 8 : 6), 2, LAY_P2S>();
+      // sample and difference planes, two items per FP32x2 instruction
+      if (variant == 26) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_X3, METHOD == METHOD_CRS, 512, 2>();
+      if (variant == 27) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_X3, METHOD == METHOD_CRS, 512>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();

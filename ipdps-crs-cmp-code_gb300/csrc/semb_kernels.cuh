@@ -229,6 +229,14 @@ constexpr int kMaxNsFT = 8192;
 // FMAs (no (x, x) operand).
 constexpr int LAY_PD5 = 7;
 constexpr int LAY_PD5S = 8;
+// w = 3, pipelined kernel only: two planes of floats per stage, the samples s_k and
+// their differences d_k = s_k+1 - s_k, the difference plane kXPlane floats after the
+// sample plane.  An item reads s_k, s_k+2, d_k, d_k+2 with four 32-bit loads (four
+// shared-memory wavefronts per warp, as one 16-byte entry), and two items of a
+// thread share every FP32x2 instruction: lane .x holds item 2p, lane .y item 2p+1,
+// so the window arithmetic is packed throughout and needs no (x, x) operand.
+constexpr int LAY_X3 = 9;
+constexpr int kXPlane = 4096;
 
 // layout of the staged entries of an accumulation layout
 __host__ __device__ constexpr int stage_lay(int lay) {
@@ -241,9 +249,9 @@ __host__ __device__ constexpr bool lay_has_side(int lay) {
 }
 
 // bytes of one staged entry (the address stride of an item's window), and of one
-// staged sample with its side entry (LAY_FT, LAY_PD5)
-__host__ __device__ constexpr int lay_entry_bytes(int) { return 16; }
-__host__ __device__ constexpr int lay_stage_bytes(int lay) { return lay_has_side(lay) ? 24 : 16; }
+// staged sample with its side entry (LAY_FT, LAY_PD5) or its difference (LAY_X3)
+__host__ __device__ constexpr int lay_entry_bytes(int lay) { return lay == LAY_X3 ? 4 : 16; }
+__host__ __device__ constexpr int lay_stage_bytes(int lay) { return lay_has_side(lay) ? 24 : lay == LAY_X3 ? 8 : 16; }
 
 struct ChunkMeta {
   float4 geo[kMaxChunk];   // (|dm|, dm^2, h, soff as int bits)
@@ -507,6 +515,25 @@ __device__ __forceinline__ void convert_chunk(const KParams& P, const ChunkMeta*
     const float* r32 = reinterpret_cast<const float*>(raw) + roff;
     const uint16_t* r16 = reinterpret_cast<const uint16_t*>(raw) + roff;
     const bool f16 = P.storage == STORE_F16;
+    if constexpr (LAY == LAY_X3) {
+      // the sample and difference planes
+      float* S = reinterpret_cast<float*>(bufq) + si.w;
+      for (int k = lane; k < si.z; k += 32) {
+        float v[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (P.storage == STORE_F32) {
+            v[u] = r32[k + u];
+          } else {
+            const uint32_t b = r16[k + u];
+            v[u] = (f16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
+          }
+        }
+        S[k] = v[0];
+        S[kXPlane + k] = v[1] - v[0];
+      }
+      continue;
+    }
     if constexpr (stage_lay(LAY) == LAY_FT) {
       // values pre-offset by the window's integer sample (absolute index lo + k + tau)
       float2* side = reinterpret_cast<float2*>(bufq + P.cap + kZeroSlots) + si.w;
@@ -566,6 +593,12 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, uint64_
 __device__ __forceinline__ float4 lds128(uint32_t a) {
   float4 v;
   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+  return v;
+}
+
+__device__ __forceinline__ float lds32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
   return v;
 }
 
@@ -927,6 +960,92 @@ struct FastAcc<W, LAY_FT> {
 
 
 
+
+// The RC item accumulators of one thread.  For the 16-byte and side-entry layouts
+// an array of FastAcc, one per item; set[r] is item r.
+template <int W, int LAY, int RC>
+struct AccSet {
+  FastAcc<W, LAY> a[RC];
+  __device__ __forceinline__ FastAcc<W, LAY>& operator[](int r) { return a[r]; }
+};
+
+// LAY_X3 (w = 3): the sums of items 2p and 2p+1 share FP32x2 registers, item 2p in
+// lane .x and item 2p+1 in lane .y.  add_pair() folds in one trace for both items of
+// pair p with packed arithmetic throughout: (s_1, d_1) are rebuilt as s_1 = s_0 + d_0
+// and d_1 = s_2 - s_1, as in LAY_PD.  set[r] is a view of item r with the per-item
+// interface of FastAcc (scalar arithmetic on its lane), for the partly-in-range traces
+// and the odd item of an odd RC.
+template <int RC>
+struct AccSet<3, LAY_X3, RC> {
+  static constexpr int RP = (RC + 1) / 2;
+  static constexpr uint32_t kD = 4u * kXPlane;   // bytes from a sample to its difference
+  float2 n0[RP], n1[RP], n2[RP], den[RP];
+  int Ms[RC];
+
+  struct Item {
+    AccSet& s;
+    const int r;
+    int& M;
+    __device__ __forceinline__ float& lanev(float2& v) const { return (r & 1) ? v.y : v.x; }
+    __device__ __forceinline__ void reset() const {
+      lanev(s.n0[r >> 1]) = 0.f;
+      lanev(s.n1[r >> 1]) = 0.f;
+      lanev(s.n2[r >> 1]) = 0.f;
+      lanev(s.den[r >> 1]) = 0.f;
+      M = 0;
+    }
+    __device__ __forceinline__ void acc(float s0, float s2, float d0, float d2, float x) const {
+      const float v0 = fmaf(d0, x, s0), v2 = fmaf(d2, x, s2);
+      const float s1 = s0 + d0;
+      const float v1 = fmaf(s2 - s1, x, s1);
+      float& e = lanev(s.den[r >> 1]);
+      lanev(s.n0[r >> 1]) += v0;
+      lanev(s.n1[r >> 1]) += v1;
+      lanev(s.n2[r >> 1]) += v2;
+      e = fmaf(v0, v0, e);
+      e = fmaf(v1, v1, e);
+      e = fmaf(v2, v2, e);
+    }
+    // the window at sample address a (sample plane) with weight x
+    __device__ __forceinline__ void add(uint32_t a, float x) const {
+      acc(lds32(a), lds32(a + 8u), lds32(a + kD), lds32(a + kD + 8u), x);
+    }
+    __device__ __forceinline__ void add_samples(const float* sv, float x) const {
+      acc(sv[0], sv[2], sv[1] - sv[0], sv[3] - sv[2], x);
+    }
+    __device__ __forceinline__ float take_energy() const {
+      float& e = lanev(s.den[r >> 1]);
+      const float v = e;
+      e = 0.f;
+      return v;
+    }
+    __device__ __forceinline__ void sums(float& acsq, float& lin) const {
+      const float a0 = lanev(s.n0[r >> 1]), a1 = lanev(s.n1[r >> 1]), a2 = lanev(s.n2[r >> 1]);
+      acsq = fmaf(a0, a0, fmaf(a2, a2, a1 * a1));
+      lin = a0 + a1 + a2;
+    }
+  };
+  __device__ __forceinline__ Item operator[](int r) { return Item{*this, r, Ms[r]}; }
+
+  // one trace for items 2p (window at a0) and 2p+1 (at a1), weights x = (x_2p, x_2p+1)
+  __device__ __forceinline__ void add_pair(int p, uint32_t a0, uint32_t a1, float2 x) {
+    const float2 s0 = make_float2(lds32(a0), lds32(a1));
+    const float2 s2 = make_float2(lds32(a0 + 8u), lds32(a1 + 8u));
+    const float2 d0 = make_float2(lds32(a0 + kD), lds32(a1 + kD));
+    const float2 d2 = make_float2(lds32(a0 + kD + 8u), lds32(a1 + kD + 8u));
+    const float2 v0 = __ffma2_rn(d0, x, s0);
+    const float2 v2 = __ffma2_rn(d2, x, s2);
+    const float2 s1 = __fadd2_rn(s0, d0);
+    const float2 d1 = __ffma2_rn(s1, make_float2(-1.f, -1.f), s2);   // s_2 - s_1, exact as a subtraction
+    const float2 v1 = __ffma2_rn(d1, x, s1);
+    n0[p] = __fadd2_rn(n0[p], v0);
+    n1[p] = __fadd2_rn(n1[p], v1);
+    n2[p] = __fadd2_rn(n2[p], v2);
+    den[p] = __ffma2_rn(v0, v0, den[p]);
+    den[p] = __ffma2_rn(v1, v1, den[p]);
+    den[p] = __ffma2_rn(v2, v2, den[p]);
+  }
+};
 
 // Batched form: the items of one thread on a trace whose window was not staged
 // (kGlobalEntry): the traveltime as on the staged traces, then the window samples
