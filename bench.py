@@ -186,12 +186,16 @@ class ClockSampler:
 # ----------------------------------------------------------------------------- helpers
 
 def algo_flops(method: int, st: dict, nap: int) -> float:
-    """Algorithmic FLOPs of one search: per eval N_ap*(T + 7w) + 2w + 2 with T = 5
-    (CMP: add, mul, sqrt, scale, frac) or 10 (CRS), per window sample 3 for the
-    interpolation, 1 for num, 2 for den, 1 for lin."""
+    """Algorithmic FLOPs of one batched search: per eval N_ap*(T + 6w) + 2w + 2 with
+    T = 5 (CMP: add, mul, sqrt, scale, frac) or 10 (CRS), per window sample 3 for the
+    interpolation, 1 for num and 2 for den.  The reference also sums each window sample
+    into a separate linear sum (one more flop per sample); the batched form takes its
+    stack from the numerators instead, so that flop is not counted.  Traces that no item
+    of a pass can reach are skipped by the kernel and still counted (about 1-2% of the
+    trace-evaluations on the CRS surveys)."""
     w = st["window"]
     T = 5 if method == semb.CMP else 10
-    per_cand_t0 = nap * (T + 7 * w) + st["ncdps"] * (2 * w + 2)
+    per_cand_t0 = nap * (T + 6 * w) + st["ncdps"] * (2 * w + 2)
     return float(st["ns"]) * st["ncand"] * per_cand_t0
 
 
@@ -777,7 +781,7 @@ def main():
     ap.add_argument("--tune", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--stream-chunks", type=int, default=8, help="CDP chunks of the streamed end-to-end run")
+    ap.add_argument("--stream-chunks", type=int, default=16, help="CDP chunks of the streamed end-to-end run")
     ap.add_argument("--repick-gap", type=float, default=None,
                     help="near-tie threshold of the FP64 re-pick (default: the library's)")
     ap.add_argument("--no-cpu", action="store_true")

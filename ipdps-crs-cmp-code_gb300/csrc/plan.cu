@@ -103,6 +103,7 @@ struct semb_plan {
   float* d_ingest = nullptr;   // staging of the linear trace copies (copy_traces)
   uint16_t* d_samples16 = nullptr;
   float* d_scale = nullptr;
+  unsigned char* d_setup = nullptr;   // upload scratch arena (Scratch)
   int64_t* d_ap_off = nullptr;
   int32_t* d_ap_tr = nullptr;
   float4* d_ap_geo = nullptr;
@@ -179,17 +180,21 @@ int dev_alloc(T** p, size_t n) {
   return SEMB_OK;
 }
 
-// Device scratch freed when the guard goes out of scope (all exit paths).
+// Set-up scratch of an upload: consecutive 256-byte-aligned arrays carved from one
+// device arena that the plan keeps for the next upload (no allocation or free, and so
+// no device-wide synchronisation, when the survey's size repeats).
+constexpr size_t scratch_bytes(size_t bytes) { return ((bytes > 0 ? bytes : 1) + 255) & ~(size_t)255; }
+
 struct Scratch {
-  std::vector<void*> ptrs;
-  ~Scratch() {
-    for (void* p : ptrs) cudaFree(p);
-  }
+  unsigned char* base = nullptr;
+  size_t used = 0, cap = 0;
   template <typename T>
   int alloc(T** p, size_t n) {
-    int rc = dev_alloc(p, n);
-    if (rc == SEMB_OK) ptrs.push_back(*p);
-    return rc;
+    const size_t b = scratch_bytes(n * sizeof(T));
+    if (used + b > cap) return fail(SEMB_E_ARG, "upload scratch of %zu bytes exceeded", cap);
+    *p = reinterpret_cast<T*>(base + used);
+    used += b;
+    return SEMB_OK;
   }
 };
 
@@ -240,6 +245,7 @@ void free_data(semb_plan* pl, bool keep_reusable = false) {
   release(pl->d_ingest);
   release(pl->d_samples16);
   release(pl->d_scale);
+  release(pl->d_setup);
   release(pl->d_ap_off);
   release(pl->d_ap_tr);
   release(pl->d_ap_geo);
@@ -617,6 +623,12 @@ int semb_plan_stream(semb_plan* pl, const semb_gather_view* g, int32_t nchunks) 
   if (pl->p.mode != SEMB_BATCHED || pl->p.ngen > 0)
     return fail(SEMB_E_ARG, "the streamed search is the batched form's grid search");
   if (nchunks < 1 || nchunks > 64) return fail(SEMB_E_ARG, "nchunks must be in 1..64");
+  // the chunk copies, queued by the upload, read the caller's buffer until they end:
+  // every exit waits for them
+  struct CopyJoin {
+    cudaStream_t s;
+    ~CopyJoin() { cudaStreamSynchronize(s); }
+  } join{pl->copy_stream};
   SEMB_TRY(upload_impl(pl, g, nchunks));
   return enqueue_streamed(pl, g);
 }
@@ -703,17 +715,44 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   // 2-D transfer) and, batched, the 16-bit store built from it on the device
   cudaStream_t cs = pl->copy_stream;
   struct CopyJoin {   // every exit waits for the copies, which read the caller's buffer
-    cudaStream_t s;
-    ~CopyJoin() { cudaStreamSynchronize(s); }
-  } copy_join{cs};
+    cudaStream_t s;   // (streamed: semb_plan_stream waits for them after the search)
+    ~CopyJoin() {
+      if (s) cudaStreamSynchronize(s);
+    }
+  } copy_join{nchunks == 0 ? cs : nullptr};
   SEMB_CUDA(cudaStreamWaitEvent(cs, pl->ev[4], 0));
   SEMB_TRY(dev_reuse(pl, &pl->d_samples, (size_t)ntr * pl->pitch));
   if (p.mode == SEMB_BATCHED && p.storage != SEMB_STORE_F32) {
     SEMB_TRY(dev_reuse(pl, &pl->d_samples16, (size_t)ntr * pl->pitch));
     SEMB_TRY(dev_reuse(pl, &pl->d_scale, ntr));
   }
-  if (nchunks == 0) SEMB_TRY(copy_traces(pl, g, 0, ntr, cs));   // streamed: per chunk in the run
+  if (nchunks == 0) SEMB_TRY(copy_traces(pl, g, 0, ntr, cs));
   SEMB_CUDA(cudaEventRecord(pl->copy_done, cs));
+  pl->nchunks = nchunks;
+  if (nchunks > 0) {
+    // streamed: CDP chunks of about equal trace counts in gather order.  Every chunk's
+    // copies are queued now, so that they run during the set-up below and during the
+    // search of the chunks before them; chunk_done[k] marks chunk k's traces in place.
+    pl->chunk_cdp.assign(1, 0);
+    for (int k = 1; k < nchunks; ++k) {
+      const int64_t target = g->ntraces * k / nchunks;
+      int c = pl->chunk_cdp.back();
+      while (c < g->ncdps && g->cdp_end[c] <= target) ++c;
+      pl->chunk_cdp.push_back(std::max(c, pl->chunk_cdp.back()));
+    }
+    pl->chunk_cdp.push_back(g->ncdps);
+    while ((int)pl->chunk_done.size() < nchunks) {
+      cudaEvent_t e;
+      SEMB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      pl->chunk_done.push_back(e);
+    }
+    for (int k = 0; k < nchunks; ++k) {
+      const int c0 = pl->chunk_cdp[k], c1 = pl->chunk_cdp[k + 1];
+      const int64_t t0 = c0 > 0 ? g->cdp_end[c0 - 1] : 0, t1 = c1 > 0 ? g->cdp_end[c1 - 1] : 0;
+      SEMB_TRY(copy_traces(pl, g, t0, t1, cs));
+      SEMB_CUDA(cudaEventRecord(pl->chunk_done[k], cs));
+    }
+  }
 
   // header fields and CDP ranges (scratch for the set-up kernels)
   int32_t *d_gx, *d_gy, *d_sx, *d_sy, *d_sc;
@@ -723,6 +762,13 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   int32_t* d_cnt32;
   int64_t* d_cnt64;
   Scratch scratch;
+  {
+    const size_t ncd = (size_t)g->ncdps, nt = (size_t)ntr;
+    scratch.cap = 8 * scratch_bytes(nt * 4) + 3 * scratch_bytes(nt * 8) + 3 * scratch_bytes(ncd * 4) +
+                  2 * scratch_bytes(ncd * 8);
+    SEMB_TRY(dev_reuse(pl, &pl->d_setup, scratch.cap));
+    scratch.base = pl->d_setup;
+  }
   SEMB_TRY(scratch.alloc(&d_gx, ntr));
   SEMB_TRY(scratch.alloc(&d_gy, ntr));
   SEMB_TRY(scratch.alloc(&d_sx, ntr));
@@ -774,7 +820,7 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
     for (int i = 0; i <= g->ncdps; ++i) off[i] = i;
     std::iota(lst.begin(), lst.end(), 0);
     pl->n_nbr = g->ncdps;
-    SEMB_TRY(dev_alloc(&pl->d_nbr, g->ncdps));
+    SEMB_TRY(dev_reuse(pl, &pl->d_nbr, g->ncdps));
     SEMB_CUDA(cudaMemcpyAsync(pl->d_nbr_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice, st));
     SEMB_CUDA(cudaMemcpyAsync(pl->d_nbr, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice, st));
     SEMB_CUDA(cudaStreamSynchronize(st));
@@ -825,7 +871,7 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
         for (int ib = 0; ib < p.nb; ++ib) pl->order[q++] = ia * p.nb * p.nc + ib * p.nc + ic;
   }
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  SEMB_TRY(dev_alloc(&pl->d_cand64, pl->g64.size()));
+  SEMB_TRY(dev_reuse(pl, &pl->d_cand64, pl->g64.size()));
   SEMB_CUDA(cudaMemcpyAsync(pl->d_cand64, pl->g64.data(), pl->g64.size() * 8, cudaMemcpyHostToDevice, st));
 
   // work queue: (cdp, t0 block), largest aperture first (longest-processing-time order)
@@ -839,22 +885,12 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   if (ntasks >= INT32_MAX) return fail(SEMB_E_ARG, "too many tasks");
   std::vector<int2> tasks((size_t)ntasks);
   size_t q = 0;
-  pl->nchunks = nchunks;
   if (nchunks == 0) {
     for (int c : cdp_order)
       for (int b = 0; b < nblk; ++b) tasks[q++] = make_int2(c, b * kTB);
   } else {
-    // streamed: CDP chunks of about equal trace counts in gather order, each chunk's
-    // tasks longest aperture first; chunk k's search waits for the copies of the
-    // last chunk its apertures read (chunk_need)
-    pl->chunk_cdp.assign(1, 0);
-    for (int k = 1; k < nchunks; ++k) {
-      const int64_t target = g->ntraces * k / nchunks;
-      int c = pl->chunk_cdp.back();
-      while (c < g->ncdps && g->cdp_end[c] <= target) ++c;
-      pl->chunk_cdp.push_back(std::max(c, pl->chunk_cdp.back()));
-    }
-    pl->chunk_cdp.push_back(g->ncdps);
+    // streamed: each chunk's tasks longest aperture first; chunk k's search waits for
+    // the copies of the last chunk its apertures read (chunk_need)
     std::vector<int> chunk_of(g->ncdps);
     for (int k = 0; k < nchunks; ++k)
       for (int c = pl->chunk_cdp[k]; c < pl->chunk_cdp[k + 1]; ++c) chunk_of[c] = k;
@@ -1161,22 +1197,11 @@ int enqueue_streamed(semb_plan* pl, const semb_gather_view* g) {
     ~CopyJoin() { cudaStreamSynchronize(s); }
   } join{cs};
   const int nk = pl->nchunks;
-  while ((int)pl->chunk_done.size() < nk) {
-    cudaEvent_t e;
-    SEMB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    pl->chunk_done.push_back(e);
-  }
+  (void)g;   // the chunk copies were queued by the upload (upload_impl)
   SEMB_TRY(dev_reuse(pl, &pl->d_chunk_counter, nk));
   SEMB_CUDA(cudaMemsetAsync(pl->d_status, 0, kStatusWords * sizeof(int), st));
   SEMB_CUDA(cudaMemsetAsync(pl->d_chunk_counter, 0, nk * sizeof(int), st));
   SEMB_CUDA(cudaEventRecord(pl->ev[0], st));
-  SEMB_CUDA(cudaStreamWaitEvent(cs, pl->ev[0], 0));
-  for (int k = 0; k < nk; ++k) {
-    const int c0 = pl->chunk_cdp[k], c1 = pl->chunk_cdp[k + 1];
-    const int64_t t0 = c0 > 0 ? g->cdp_end[c0 - 1] : 0, t1 = c1 > 0 ? g->cdp_end[c1 - 1] : 0;
-    SEMB_TRY(copy_traces(pl, g, t0, t1, cs));
-    SEMB_CUDA(cudaEventRecord(pl->chunk_done[k], cs));
-  }
   const Bucket& b = pl->buckets[0];
   const int form = FORM_FAST;
   int launches = 0;
