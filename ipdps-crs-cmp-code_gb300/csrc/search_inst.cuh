@@ -130,6 +130,9 @@ SearchEntry search_entry(int w, int variant) {
       // sample and difference planes, two items per FP32x2 instruction
       if (variant == 26) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_X3, METHOD == METHOD_CRS, 512, 2>();
       if (variant == 27) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_X3, METHOD == METHOD_CRS, 512>();
+      // variant 13 with 640 threads (20 warps per SM) at whole-trace stages
+      if (variant == 28) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 640, 2>();
+      if (variant == 29) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 640>();
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
