@@ -185,18 +185,29 @@ class ClockSampler:
 
 # ----------------------------------------------------------------------------- helpers
 
-def algo_flops(method: int, st: dict, nap: int) -> float:
-    """Algorithmic FLOPs of one batched search: per eval N_ap*(T + 6w) + 2w + 2 with
-    T = 5 (CMP: add, mul, sqrt, scale, frac) or 10 (CRS), per window sample 3 for the
-    interpolation, 1 for num and 2 for den.  The reference also sums each window sample
-    into a separate linear sum (one more flop per sample); the batched form takes its
-    stack from the numerators instead, so that flop is not counted.  Traces that no item
-    of a pass can reach are skipped by the kernel and still counted (about 1-2% of the
+def algo_flops(method: int, st: dict, nap: int, lin: bool = True) -> float:
+    """Algorithmic FLOPs of one search: per eval N_ap*(T + 7w) + 2w + 2 with T = 5
+    (CMP: add, mul, sqrt, scale, frac) or 10 (CRS), per window sample 3 for the
+    interpolation, 1 for num, 2 for den and 1 for the reference's linear sum (the
+    algorithm's count, which `roofline.achieved` uses).  lin=False leaves the linear
+    sum out: the batched form takes its stack from the numerators, so this is the
+    count of the operations it performs (`roofline.achieved_own_ops`).  Both count the
+    traces that no item of a pass can reach, which the kernel skips (about 1-2% of the
     trace-evaluations on the CRS surveys)."""
     w = st["window"]
     T = 5 if method == semb.CMP else 10
-    per_cand_t0 = nap * (T + 6 * w) + st["ncdps"] * (2 * w + 2)
+    per_cand_t0 = nap * (T + (7 if lin else 6) * w) + st["ncdps"] * (2 * w + 2)
     return float(st["ns"]) * st["ncand"] * per_cand_t0
+
+
+def fp32_roofline(method: int, st: dict, nap: int, ms: float, peak: float) -> dict:
+    """The FP32 side of the roofline of a batched search that took `ms`: the
+    algorithm's FLOP/s and the batched form's own, against the live FMA-rate probe."""
+    ach = algo_flops(method, st, nap) / (ms * 1e-3) / 1e12
+    own = algo_flops(method, st, nap, lin=False) / (ms * 1e-3) / 1e12
+    return {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+            "achieved_own_ops": own, "frac_own_ops": own / peak,
+            "peak_source": "measured live: semb_probe_fp32 FMA throughput"}
 
 
 def timed_runs(plan: semb.Plan, warmup: int, steps: int):
@@ -471,11 +482,7 @@ def run_target(args, dev):
     out["plain"] = {"ms": pst["ms_total"], "evals_per_s": pst["evals"] / (pst["ms_total"] * 1e-3)}
     out["ratio"] = pst["ms_total"] / st["ms_total"]
     out["met"] = bool(out["ratio"] >= TARGET_RATIO)
-    flops = algo_flops(method, st, nap)
-    peak = semb.probe_fp32_tflops(dev)
-    ach = flops / (st["ms_search"] * 1e-3) / 1e12
-    out["roofline"] = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                       "peak_source": "measured live: semb_probe_fp32 FMA throughput"}
+    out["roofline"] = fp32_roofline(method, st, nap, st["ms_search"], semb.probe_fp32_tflops(dev))
     if not args.no_cpu:
         oracle = oracle_mod()
         idx = bucket_sample(ap, per_bucket=args.target_err_per_bucket, seed=11)
@@ -544,17 +551,14 @@ def run_chunked_survey(args):
         ap = plan.download_attrs(batched=False)["aperture"]
         ctr, sem, stk = plan.download()
     nap = int(ap.sum())
-    flops = algo_flops(method, st, nap)
-    peak = semb.probe_fp32_tflops(dev)
     total_ms = st["ms_total"]
-    ach = flops / (total_ms * 1e-3) / 1e12
+    roof = fp32_roofline(method, st, nap, total_ms, semb.probe_fp32_tflops(dev))
+    roof["note"] = "search + re-pick time of every chunk (graph replays give no split)"
     out.update(ncand=st["ncand"], window=st["window"], mean_aperture=float(ap.mean()), evals=st["evals"],
                trace_evals=st["trace_evals"], ms_total=total_ms, chunks=len(chunk_ms), ms_per_chunk=chunk_ms,
                evals_per_s=st["evals"] / (total_ms * 1e-3), repicked=st["repicked"],
                kernel_launches=st["kernel_launches"], clocks=clk.summary(),
-               roofline={"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                         "note": "search + re-pick time of every chunk (graph replays give no split)",
-                         "peak_source": "measured live: semb_probe_fp32 FMA throughput"})
+               roofline=roof)
     if child is not None:
         _, status = os.waitpid(child, 0)
         if status == 0 and os.path.exists(err_path):
@@ -716,7 +720,6 @@ def run_ours(args, rank, world, dist):
                "sample": f"{text}, {secs:.1f} s of CPU search (oracle restatement, OpenMP)"}
 
     peak = semb.probe_fp32_tflops(dev)
-    achieved = flops / (ms_search * 1e-3) / 1e12
     traffic = traffic_from_profiles(args.workload, st["ncdps"], st["trace_evals"])
     hbm = None
     if traffic is not None:
@@ -730,11 +733,9 @@ def run_ours(args, rank, world, dist):
         got = traffic / (ms_search * 1e-3) / 1e9
         hbm = {"achieved_gbs": got, "peak_gbs": hbm_peak, "frac": got / hbm_peak if hbm_peak else None,
                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)"}
-    roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "traffic": traffic, "traffic_unit": "DRAM bytes per search launch (ncu)", "hbm": hbm,
-            "smem": smem_from_profiles(args.workload),
-            "peak_source": "measured live: semb_probe_fp32 FMA throughput",
-            "flops_per_launch": flops, "launch_ms": ms_search}
+    roof = fp32_roofline(method, st, nap, ms_search, peak)
+    roof.update({"traffic": traffic, "traffic_unit": "DRAM bytes per search launch (ncu)", "hbm": hbm,
+                 "smem": smem_from_profiles(args.workload), "flops_per_launch": flops, "launch_ms": ms_search})
     clocks = clk.summary()
     cfg = workload_config(args.workload, s, method, world, nap / st["ncdps"])
     line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
