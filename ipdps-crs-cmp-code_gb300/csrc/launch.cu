@@ -18,7 +18,7 @@ static SearchEntry lookup(int method, int form, int w, int v) {
 }
 
 int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* brun, int* nt, int* pipe, int* lay,
-                   int* glob) {
+                   int* glob, int* z0) {
   if (v < 0 || v >= kMaxVariants) return 0;
   SearchEntry e = lookup(method, form, w, v);
   *rc = e.rc;
@@ -28,20 +28,28 @@ int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* 
   if (pipe) *pipe = e.pipe;
   if (lay) *lay = e.lay;
   if (glob) *glob = e.glob;
+  if (z0) *z0 = e.z0;
   return e.fn != nullptr;
 }
 
 // Variant a plan starts with (before any autotuning), the fastest measured on GB300
 // for the benchmark workloads of each window: for CRS the pipelined 512-thread B-run
-// kernel (packed value/difference staging with a two-way trace unroll for w = 3,
-// packed pairs otherwise); for CMP the two-barrier kernel with packed pairs (w = 3)
-// or packed pairs formed by scalar FMAs (w = 5); variant 0 elsewhere.
+// kernel (packed value/difference staging with a two-way trace unroll and the central
+// traces' sums shared over A and B for w = 3, packed pairs otherwise); for CMP the
+// two-barrier kernel with packed pairs (w = 3) or packed pairs formed by scalar FMAs
+// (w = 5); variant 0 elsewhere.  fallback_variant() is the one to use where the default
+// does not fit the plan (a grid whose passes span more C values than variant 30 takes).
 int default_variant(int method, int form, int w) {
   if (form != FORM_FAST) return 0;
-  if (method == METHOD_CRS && w == 3) return 13;
+  if (method == METHOD_CRS && w == 3) return 30;
   if (method == METHOD_CRS && w <= 5) return 14;
   if (method == METHOD_CMP && w == 3) return 8;
   if (method == METHOD_CMP && w == 5) return 21;
+  return 0;
+}
+
+int fallback_variant(int method, int form, int w) {
+  if (form == FORM_FAST && method == METHOD_CRS && w == 3) return 13;
   return 0;
 }
 

@@ -44,7 +44,8 @@ struct ChunkTag {
   int t0s;
   int pass;
   int napert;
-  int pad[3];
+  int ic_lo;   // Z0: the pass's first C index (its central sums are in the chunk's z0 slot)
+  int pad[2];
 };
 
 // The planners' position in the chunk stream.
@@ -55,6 +56,7 @@ struct Producer {
   int done;   // the end-of-stream chunk has been issued
   int next;   // index of the next chunk to produce
   float T_lo, T_hi;
+  int64_t zb, ze;   // Z0: the task's central traces (entries zb .. ze-1)
 };
 
 // Shared-memory layout (bytes), shared by host and device:
@@ -67,17 +69,22 @@ struct Producer {
 //   kahan      Kahan totals and compensations [2][RC][NT]
 //   quad[3]    staged 16-byte entries, each followed by its zero block
 //   raw[2]     raw windows (TMA destination)
+//   z0[4]      Z0 variants: the central traces' sums carried by a pass's last chunk,
+//              [kZ0C][5][32] floats per chunk slot
 struct PipeLayout {
-  size_t prod, meta, tag, src, tops, kahan, quad, quad_stride, raw, raw_stride, total;
+  size_t prod, meta, tag, src, z0, tops, kahan, quad, quad_stride, raw, raw_stride, total;
 };
 
-__host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, int nt, int lay) {
+constexpr size_t kZ0SlotFloats = (size_t)kZ0C * 5 * 32;
+
+__host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, int nt, int lay, int z0 = 0) {
   PipeLayout L;
   L.prod = 128;
   L.meta = L.prod + align128(sizeof(Producer));
   L.tag = L.meta + kMetaRing * kMetaBytes;
   L.src = L.tag + align128(kMetaRing * sizeof(ChunkTag));
-  L.tops = L.src + (size_t)kMetaRing * kMaxChunk * 16;
+  L.z0 = L.src + (size_t)kMetaRing * kMaxChunk * 16;
+  L.tops = L.z0 + (z0 ? (size_t)kMetaRing * kZ0SlotFloats * 4 : 0);
   L.kahan = L.tops + align128(3 * (size_t)kTopK * nt * 4);
   L.quad = L.kahan + align128(2 * (size_t)rc * nt * 4);
   // LAY_X3: a sample plane and a difference plane of kXPlane floats each (the plan
@@ -93,13 +100,86 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// Z0 (CRS, w = 3): the sums of a task's central traces at zero midpoint distance,
+// which every (A, B) of one C shares: with |dm| = 0 an item's traveltime is
+// t^2 = fma(t0, t0, C h) whatever A and B.  Computed with the items' own FP32
+// operations (the traveltime, its sample index and weight, and the interpolation of the
+// packed value/difference staging), so each trace adds what it would add to every
+// item of that C.  One lane per t0 of the task (lane = t0 - t0s), C indices c_lo ..
+// c_lo + nc - 1; slot[(ci * 5 + q) * 32 + lane] holds the three window numerators, the
+// energy and the count of in-range traces (as a float).  Samples are read from the
+// trace store in global memory, within each trace's row (an in-range window ends at
+// most two samples past the record, inside the row's zero padding); a CDP's own traces
+// are consecutive in the store and in its aperture list.
+static __device__ __noinline__ void central_sums(const KParams& P, int t0s, int64_t zb, int64_t ze, int c_lo, int nc,
+                                                 float* slot) {
+  const int lane = threadIdx.x & 31;
+  const float T = (float)min(t0s + lane, P.ns - 1);
+  const unsigned span = (unsigned)(P.ns - 2 * P.tau - 2);
+  const int tr0 = zb < ze ? __ldg(P.ap_tr + zb) : 0;
+  for (int ci = 0; ci < nc; ++ci) {
+    const float cc = P.cvals[c_lo + ci];
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f, den = 0.f, m = 0.f;
+    for (int64_t k = zb; k < ze; ++k) {
+      const float4 g = __ldg(P.ap_geo + k);
+      if (g.x != 0.f) continue;
+      const float t = sqrt_fast(fmaf(T, T, cc * g.z));
+      const float y = __fadd_rz(t, 8388608.0f);
+      const int rel = __float_as_int(y) - (0x4B000000 + P.tau);   // it - tau
+      if ((unsigned)rel > span) continue;
+      const float x = t - (y - 8388608.0f);
+      const int tr = tr0 + (int)(k - zb);
+      const int64_t at = (int64_t)tr * P.pitch + rel;
+      float v[4];
+      if (P.storage == STORE_F32) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = __ldg(P.samples + at + u);
+      } else {
+        const float sc = __ldg(P.scale + tr);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint32_t b = __ldg(P.samples16 + at + u);
+          v[u] = (P.storage == STORE_F16 ? half_bits_to_float(b) : __uint_as_float(b << 16)) * sc;
+        }
+      }
+      // the packed value/difference entry (s_0, s_2, d_0, d_2) and its window
+      const float d0 = v[1] - v[0], d2 = v[3] - v[2];
+      const float w0 = fmaf(d0, x, v[0]), w2 = fmaf(d2, x, v[2]);
+      const float s1 = v[0] + d0;
+      const float w1 = fmaf(v[2] - s1, x, s1);
+      n0 += w0;
+      n1 += w1;
+      n2 += w2;
+      den = fmaf(w0, w0, den);
+      den = fmaf(w1, w1, den);
+      den = fmaf(w2, w2, den);
+      m += 1.f;
+    }
+    float* z = slot + ci * 5 * 32 + lane;
+    z[0] = n0;
+    z[32] = n1;
+    z[64] = n2;
+    z[96] = den;
+    z[128] = m;
+  }
+}
+
 // TU: unroll factor of the in-range trace loop (independent work of TU traces in
 // flight per iteration).
 // GLOB: as for semb_search_kernel, the variant may stage less than a whole trace.
-template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TU = 1, bool GLOB = false>
+// Z0 (CRS B-run, packed value/difference staging): the planner leaves the task's
+// central traces at zero midpoint distance out of the chunks and, when it plans a
+// pass's last chunk, computes their sums for each C index of the pass into that
+// chunk's z0 slot (central_sums); each item adds those of its C when it finalizes.
+template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TU = 1, bool GLOB = false,
+          bool Z0 = false>
 __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
+  static_assert(!Z0 || (METHOD == METHOD_CRS && BRUN && W == 3 && stage_lay(LAY) == LAY_PD),
+                "central-trace sharing is for the CRS B-run packed value/difference kernel");
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT, LAY);
+  const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT, LAY, Z0 ? 1 : 0);
+  float* z0_base = reinterpret_cast<float*>(smem_raw + L.z0);
+  auto z0_at = [&](int c) { return z0_base + (size_t)(c % kMetaRing) * kZ0SlotFloats; };
   constexpr uint32_t EB = lay_entry_bytes(LAY);   // bytes per staged entry
   uint64_t* raw_full = reinterpret_cast<uint64_t*>(smem_raw);   // [kRawBufs]
   uint64_t* q_full = raw_full + kRawBufs;                        // [kStages]
@@ -189,14 +269,27 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
         prod->pass = 0;
         prod->T_lo = P.dt * (float)td.y;
         prod->T_hi = P.dt * (float)min(td.y + kTB - 1, P.ns - 1);
+        prod->zb = prod->ze = 0;
+        if (Z0) {
+          const int2 zr = P.z0r[td.x];
+          prod->zb = prod->begin + zr.x;
+          prod->ze = prod->zb + zr.y;
+        }
       }
       __syncwarp();
     }
     const int64_t pos = prod->pos, begin = prod->begin, end = prod->end;
     const int pass = prod->pass;
     int flags = pos == begin ? CH_PASS_FIRST : 0;
-    plan_chunk<METHOD, FORM_FAST>(P, P.pass_bounds + pass * 8, pos, end, prod->T_lo, prod->T_hi, m, src);
+    plan_chunk<METHOD, FORM_FAST>(P, P.pass_bounds + pass * 8, pos, end, prod->T_lo, prod->T_hi, m, src, prod->zb,
+                                  prod->ze);
     const int64_t npos = pos + m->consumed;
+    if (Z0 && npos >= end) {
+      // the pass's last chunk carries the central traces' sums of the pass's C indices
+      const int2 pc = P.pass_c[pass];
+      central_sums(P, prod->t0s, prod->zb, prod->ze, pc.x, pc.y, z0_at(c));
+      if (lane == 0) tg->ic_lo = pc.x;
+    }
     if (lane == 0) {
       if (npos >= end) {
         flags |= CH_PASS_LAST;
@@ -459,9 +552,20 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
     const float4* cand = P.cand + tg.pass * P.cpp + warp * RC;
 #pragma unroll
     for (int r = 0; r < RC; ++r) {
+      float zden = 0.f;
+      if constexpr (Z0) {
+        // the central traces' sums of this item's C index
+        const int gi = __float_as_int(__ldg(&cand[r].w));
+        if (gi >= 0) {
+          const float* z = z0_at(c) + (gi % P.nc_grid - tg.ic_lo) * 5 * 32 + lane;
+          fa[r].add_sums(z[0], z[32], z[64]);
+          zden = z[96];
+          fa[r].M += (int)z[128];
+        }
+      }
       float acsq, lin;
       fa[r].sums(acsq, lin);
-      const float den = kahan_hi[r * NT + threadIdx.x] - kahan_lo[r * NT + threadIdx.x];
+      const float den = kahan_hi[r * NT + threadIdx.x] - kahan_lo[r * NT + threadIdx.x] + zden;
       const float mf = (float)fa[r].M;
       const int err = tg.napert - fa[r].M;
       const bool ok = (den > kEpsilonF) && (fa[r].M > 0) && (err < 2);

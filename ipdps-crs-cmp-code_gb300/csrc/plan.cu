@@ -29,7 +29,7 @@ namespace semb {
 int launch_search(int method, int form, int w, int variant, const KParams& P, int nwarps, int grid, size_t smem,
                   cudaStream_t st);
 int search_variant(int method, int form, int w, int variant, int* rc, int* minb, int* brun, int* nt, int* pipe,
-                   int* lay, int* glob = nullptr);
+                   int* lay, int* glob = nullptr, int* z0 = nullptr);
 constexpr int kVariantSlots = SEMB_MAX_VARIANTS;
 constexpr int kMaxBuckets = SEMB_MAX_BUCKETS;
 // aperture split points of the work queue (traces): buckets > 1024, 385-1024,
@@ -39,6 +39,7 @@ constexpr int kBucketAp[kBucketSplits] = {1024, 384, 128};
 static_assert(kBucketSplits + 1 <= kMaxBuckets, "bucket table");
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
 int default_variant(int method, int form, int w);
+int fallback_variant(int method, int form, int w);
 int grid_neighbours(int ncdps, const float* d_fmx, const float* d_fmy, int apm, int64_t* d_off, int32_t** d_list,
                     int64_t* n_out, cudaStream_t st);
 // CDP count from which the CRS neighbour lists come from the grid search
@@ -62,6 +63,7 @@ struct KernelCfg {
   size_t smem = 0;
   float4* d_cand = nullptr;
   float* d_pass_bounds = nullptr;
+  int2* d_pass_c = nullptr;   // Z0 variants: per pass its first C index and C-index count
 };
 
 // A contiguous range of the aperture-sorted work queue, searched by one launch
@@ -105,6 +107,8 @@ struct semb_plan {
   float* d_scale = nullptr;
   unsigned char* d_setup = nullptr;   // upload scratch arena (Scratch)
   int64_t* d_ap_off = nullptr;
+  int2* d_z0r = nullptr;      // CRS: each CDP's own traces in its aperture list (first, count)
+  float* d_cvals = nullptr;   // CRS: the C value of each C index in sample units
   int32_t* d_ap_tr = nullptr;
   float4* d_ap_geo = nullptr;
   Geo64* d_ap_geo64 = nullptr;
@@ -207,6 +211,7 @@ void dev_free(T*& p) {
 void free_cfg(KernelCfg& c) {
   dev_free(c.d_cand);
   dev_free(c.d_pass_bounds);
+  dev_free(c.d_pass_c);
   c.variant = -1;
 }
 
@@ -247,6 +252,8 @@ void free_data(semb_plan* pl, bool keep_reusable = false) {
   release(pl->d_scale);
   release(pl->d_setup);
   release(pl->d_ap_off);
+  release(pl->d_z0r);
+  release(pl->d_cvals);
   release(pl->d_ap_tr);
   release(pl->d_ap_geo);
   release(pl->d_ap_geo64);
@@ -372,8 +379,8 @@ void grid_f64(const semb_params& p, std::vector<double>& abc) {
 int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   const semb_params& p = pl->p;
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
-  int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0, lay = 0, glob = 0;
-  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe, &lay, &glob))
+  int rc = 0, minb = 0, brun = 0, nt = 0, pipe = 0, lay = 0, glob = 0, z0 = 0;
+  if (!search_variant(p.method, form, pl->w, v, &rc, &minb, &brun, &nt, &pipe, &lay, &glob, &z0))
     return fail(SEMB_E_WINDOW, "no search kernel variant %d for w = %d", v, pl->w);
   if (lay == LAY_FT && pl->ns > kMaxNsFT)
     return fail(SEMB_E_ARG, "variant %d (pre-offset values) is for ns <= %d", v, kMaxNsFT);
@@ -412,6 +419,27 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   }
   const int cpp = best_nw * rc;
   const int npass = (nslots + cpp - 1) / cpp;
+  // Z0 variants: each pass's C indices (C is outermost in the search order, so they are
+  // consecutive); a pass may span at most kZ0C of them
+  std::vector<int2> pass_c;
+  if (z0) {
+    if (p.method != SEMB_CRS || !pl->d_z0r || !pl->d_cvals)
+      return fail(SEMB_E_ARG, "variant %d (shared central traces) is for CRS plans", v);
+    for (int q = 0; q < npass; ++q) {
+      int lo = INT32_MAX, hi = -1;
+      for (int k = q * cpp; k < std::min(nslots, (q + 1) * cpp); ++k) {
+        const int sv = slots[k];
+        const int ic = (sv >= 0 ? sv : -1 - sv) % p.nc;
+        lo = std::min(lo, ic);
+        hi = std::max(hi, ic);
+      }
+      if (hi < lo) lo = hi = 0;
+      if (hi - lo + 1 > kZ0C)
+        return fail(SEMB_E_ARG, "variant %d (shared central traces): a pass spans %d C values (at most %d)", v,
+                    hi - lo + 1, kZ0C);
+      pass_c.push_back(make_int2(lo, hi - lo + 1));
+    }
+  }
 
   // staging capacity, shared memory and residency, checked before the plan's
   // device state changes (a variant that does not fit leaves the plan as it was)
@@ -427,7 +455,7 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
   int cap = form == FORM_PLAIN ? 32768 : 8192;
   if (form == FORM_FAST && pl->stage_cap > 0) cap = std::min(cap, pl->stage_cap);
   auto smem_of = [&](int cp) {
-    return pipe ? pipe_layout(rc, cp, store, nt, lay).total : smem_layout(form, rc, cp, store, nt, lay).total;
+    return pipe ? pipe_layout(rc, cp, store, nt, lay, z0).total : smem_layout(form, rc, cp, store, nt, lay).total;
   };
   if (lay == LAY_X3) cap = std::min(cap, kXPlane - kZeroSlots);
   while (cap > 64 && smem_of(cap) > budget) cap -= 64;
@@ -475,13 +503,16 @@ int build_cfg(semb_plan* pl, int v, KernelCfg& out) {
     }
   }
   KernelCfg c;
-  if (dev_alloc(&c.d_cand, npad) != SEMB_OK || dev_alloc(&c.d_pass_bounds, bounds.size()) != SEMB_OK) {
+  if (dev_alloc(&c.d_cand, npad) != SEMB_OK || dev_alloc(&c.d_pass_bounds, bounds.size()) != SEMB_OK ||
+      (z0 && dev_alloc(&c.d_pass_c, pass_c.size()) != SEMB_OK)) {
     free_cfg(c);
     return fail(SEMB_E_NOMEM, "candidate table of %d entries", npad);
   }
   cudaError_t e = cudaMemcpyAsync(c.d_cand, cand.data(), npad * sizeof(float4), cudaMemcpyHostToDevice, pl->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(c.d_pass_bounds, bounds.data(), bounds.size() * 4, cudaMemcpyHostToDevice, pl->stream);
+  if (e == cudaSuccess && z0)
+    e = cudaMemcpyAsync(c.d_pass_c, pass_c.data(), pass_c.size() * sizeof(int2), cudaMemcpyHostToDevice, pl->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
   if (e != cudaSuccess) {
     free_cfg(c);
@@ -847,6 +878,11 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
                                                        p.dm_mode == SEMB_DM_SIGNED ? 1 : 0, (float)cos_d,
                                                        (float)sin_d, cos_d, sin_d);
   SEMB_CUDA(cudaGetLastError());
+  if (p.method == SEMB_CRS) {
+    SEMB_TRY(dev_reuse(pl, &pl->d_z0r, g->ncdps));
+    k_central_range<<<nc_blocks, 256, 0, st>>>(g->ncdps, pl->d_nbr_off, pl->d_nbr, d_cdp_end, pl->d_z0r);
+    SEMB_CUDA(cudaGetLastError());
+  }
   int max_ap = 0;
   for (int i = 0; i < g->ncdps; ++i) max_ap = std::max<int64_t>(max_ap, ap_off[i + 1] - ap_off[i]);
   pl->max_ap = max_ap;
@@ -873,6 +909,15 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   const int form = p.mode == SEMB_PLAIN_F32 ? FORM_PLAIN : FORM_FAST;
   SEMB_TRY(dev_reuse(pl, &pl->d_cand64, pl->g64.size()));
   SEMB_CUDA(cudaMemcpyAsync(pl->d_cand64, pl->g64.data(), pl->g64.size() * 8, cudaMemcpyHostToDevice, st));
+  if (p.method == SEMB_CRS) {
+    // the C value of C index ic in sample units, as the candidate table holds it (grid
+    // index ic: A and B at their first values)
+    std::vector<float> cv(p.nc);
+    for (int ic = 0; ic < p.nc; ++ic) cv[ic] = (float)(pl->g64[3 * (size_t)ic + 2] * (pl->idt64 * pl->idt64));
+    SEMB_TRY(dev_reuse(pl, &pl->d_cvals, cv.size()));
+    SEMB_CUDA(cudaMemcpyAsync(pl->d_cvals, cv.data(), cv.size() * 4, cudaMemcpyHostToDevice, st));
+    SEMB_CUDA(cudaStreamSynchronize(st));   // cv is a host temporary
+  }
 
   // work queue: (cdp, t0 block), largest aperture first (longest-processing-time order)
   const int nblk = (g->ns + kTB - 1) / kTB;
@@ -993,7 +1038,9 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   for (int i = 0; i < g->ncdps; ++i) pl->aperture[i] = (int32_t)(ap_off[i + 1] - ap_off[i]);
 
   // the default variant of this method and window; variant 0 where it does not fit
-  if (set_all(pl, default_variant(p.method, form, pl->w)) != SEMB_OK) SEMB_TRY(set_all(pl, 0));
+  if (set_all(pl, default_variant(p.method, form, pl->w)) != SEMB_OK &&
+      set_all(pl, fallback_variant(p.method, form, pl->w)) != SEMB_OK)
+    SEMB_TRY(set_all(pl, 0));
   SEMB_CUDA(cudaStreamWaitEvent(st, pl->copy_done, 0));   // the stores are complete for the run
   cudaEventRecord(pl->ev[5], st);
   SEMB_CUDA(cudaStreamSynchronize(st));
@@ -1029,6 +1076,10 @@ KParams make_kparams_cfg(semb_plan* pl, const KernelCfg& cfg, const int2* tasks,
   P.ap_geo = pl->d_ap_geo;
   P.cand = cfg.d_cand;
   P.pass_bounds = cfg.d_pass_bounds;
+  P.z0r = pl->d_z0r;
+  P.cvals = pl->d_cvals;
+  P.pass_c = cfg.d_pass_c;
+  P.nc_grid = pl->p.nc;
   P.npass = cfg.npass;
   P.cpp = cfg.cpp;
   P.tasks = tasks;

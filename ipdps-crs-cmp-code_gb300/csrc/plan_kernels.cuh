@@ -206,6 +206,28 @@ static __global__ void k_aperture_fill(int ncdps, int method, const int64_t* __r
   }
 }
 
+// CRS: where each CDP's own traces sit in its aperture list (k_aperture_fill appends
+// the neighbours' traces in list order, the CDP itself among them): (first entry
+// relative to ap_off[i], count).  (0, 0) if the CDP is not in its own list.
+static __global__ void k_central_range(int ncdps, const int64_t* __restrict__ nbr_off,
+                                       const int32_t* __restrict__ nbr, const int64_t* __restrict__ cdp_end,
+                                       int2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncdps) return;
+  int64_t rel = 0;
+  int2 r = make_int2(0, 0);
+  for (int64_t q = nbr_off[i]; q < nbr_off[i + 1]; ++q) {
+    const int j = nbr[q];
+    const int64_t f = cdp_end[j] - (j > 0 ? cdp_end[j - 1] : 0);
+    if (j == i) {
+      r = make_int2((int)rel, (int)f);
+      break;
+    }
+    rel += f;
+  }
+  out[i] = r;
+}
+
 // Traces copied linearly (ns samples each, back to back, as the caller holds them)
 // into the device stores: the FP32 rows at the plan's pitch with their zero padding
 // and, for a 16-bit batched store (s16 not null), the FP16/BF16 rows of the samples

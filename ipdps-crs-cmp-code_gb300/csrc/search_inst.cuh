@@ -34,6 +34,7 @@ struct SearchEntry {
   int pipe;   // 1: semb_pipe_kernel (decoupled staging ring), 0: semb_search_kernel
   int lay;    // staging layout (LAY_*)
   int glob;   // 1: stages may be smaller than a trace (long windows read global memory)
+  int z0;     // 1: the central traces' sums are shared over A and B (semb_pipe_kernel Z0)
 };
 
 constexpr int kMaxVariants = SEMB_MAX_VARIANTS;
@@ -42,7 +43,7 @@ template <int METHOD, int FORM, int W, int RC, int MINB, int LAY = LAY_QUAD, boo
           bool GLOB = false, bool XP = false>
 SearchEntry entry() {
   return {(const void*)semb_search_kernel<METHOD, FORM, W, RC, MINB, LAY, BRUN, NT, GLOB, XP>, RC, MINB, BRUN ? 1 : 0,
-          NT, 0, LAY, GLOB ? 1 : 0};
+          NT, 0, LAY, GLOB ? 1 : 0, 0};
 }
 
 // the two-barrier batched kernel with its chunk stream run on across passes and tasks
@@ -52,10 +53,10 @@ SearchEntry xp_entry() {
 }
 
 template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256, int TU = 1,
-          bool GLOB = false>
+          bool GLOB = false, bool Z0 = false>
 SearchEntry pipe_entry() {
-  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT, TU, GLOB>, RC, MINB, BRUN ? 1 : 0, NT, 1, LAY,
-          GLOB ? 1 : 0};
+  return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT, TU, GLOB, Z0>, RC, MINB, BRUN ? 1 : 0, NT, 1,
+          LAY, GLOB ? 1 : 0, Z0 ? 1 : 0};
 }
 
 // Plain form: one variant per window.
@@ -68,7 +69,7 @@ SearchEntry plain_entry() {
 template <int METHOD, int FORM>
 SearchEntry search_entry(int w, int variant) {
   if constexpr (FORM == FORM_PLAIN) {
-    if (variant != 0) return {nullptr, 0, 0, 0, 0, 0, 0, 0};
+    if (variant != 0) return {nullptr, 0, 0, 0, 0, 0, 0, 0, 0};
     switch (w) {
       case 1: return plain_entry<METHOD, 1>();
       case 3: return plain_entry<METHOD, 3>();
@@ -80,7 +81,7 @@ SearchEntry search_entry(int w, int variant) {
       case 13: return plain_entry<METHOD, 13>();
       case 15: return plain_entry<METHOD, 15>();
 #endif
-      default: return {nullptr, 0, 0, 0, 0, 0, 0, 0};
+      default: return {nullptr, 0, 0, 0, 0, 0, 0, 0, 0};
     }
   } else {
   // fast form
@@ -133,6 +134,10 @@ SearchEntry search_entry(int w, int variant) {
       // variant 13 with 640 threads (20 warps per SM) at whole-trace stages
       if (variant == 28) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 640, 2>();
       if (variant == 29) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 640>();
+      // variant 13 with the central traces' sums shared over A and B
+      if constexpr (METHOD == METHOD_CRS) {
+        if (variant == 30) return pipe_entry<METHOD, 3, 7, 1, LAY_PD, true, 512, 2, false, true>();
+      }
       break;
     case 5:
       if (variant == 0) return entry<METHOD, FORM, 5, (METHOD == METHOD_CMP ? 8 : 6), 2>();
@@ -174,7 +179,7 @@ SearchEntry search_entry(int w, int variant) {
 #endif
     default: break;
   }
-  return {nullptr, 0, 0, 0, 0, 0, 0, 0};
+  return {nullptr, 0, 0, 0, 0, 0, 0, 0, 0};
   }
 }
 

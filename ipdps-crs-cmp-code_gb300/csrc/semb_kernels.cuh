@@ -121,7 +121,18 @@ struct KParams {
   int32_t* top_idx;
   float* top_stk;
   int* status;
+  // CRS, variants that share the central CDP's traces over A and B (Z0): per CDP the
+  // (first entry, count) of its own traces in its aperture list, relative to ap_off;
+  // the C value of each C index in sample units; per pass its first C index and the
+  // number of C indices it spans (at most kZ0C)
+  const int2* z0r;
+  const float* cvals;
+  const int2* pass_c;
+  int nc_grid;
 };
+
+// Z0 variants: the most C indices one pass may span
+constexpr int kZ0C = 4;
 
 // ---------------------------------------------------------------------------
 // small PTX helpers (mbarrier + bulk copy)
@@ -375,7 +386,7 @@ __device__ __forceinline__ bool trace_window(const float* pb, float4 g, float T_
 // (plain) or one 16-byte entry per sample (fast).
 template <int METHOD, int FORM>
 __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, int64_t ap_end, float T_lo,
-                           float T_hi, ChunkMeta* meta, int4* src) {
+                           float T_hi, ChunkMeta* meta, int4* src, int64_t skip_b = 0, int64_t skip_e = 0) {
   const int lane = threadIdx.x & 31;
   constexpr int ALIGN = (FORM == FORM_PLAIN) ? 4 : 8;
   int base = 0;       // buffer units used
@@ -395,6 +406,9 @@ __device__ void plan_chunk(const KParams& P, const float* pb, int64_t ap_pos, in
     if (have) {
       g = P.ap_geo[k];
       keep = trace_window<METHOD>(pb, g, T_lo, T_hi, P.idt, P.tau, P.ns, lo, hi, inr);
+      // a trace of the central CDP at zero midpoint distance whose sums the pass shares
+      // over A and B (Z0 variants) is left out
+      if (k >= skip_b && k < skip_e && g.x == 0.f) keep = false;
       if (keep) {
         tr = P.ap_tr[k];
         if (FORM == FORM_FAST && P.storage != STORE_F32) sc = __ldg(P.scale + tr);
@@ -826,6 +840,11 @@ struct PDAcc {
     M = 0;
   }
   __device__ __forceinline__ void add(uint32_t a, float x) { acc(lds128(a), x); }
+  // window numerators computed elsewhere (the central traces' sums of a Z0 kernel)
+  __device__ __forceinline__ void add_sums(float n0, float n1, float n2) {
+    np = __fadd2_rn(np, make_float2(n0, n2));
+    ns += n1;
+  }
   // add() on window samples sv[0..3] of the FP32 store
   __device__ __forceinline__ void add_samples(const float* sv, float x) {
     acc(make_float4(sv[0], sv[2], sv[1] - sv[0], sv[3] - sv[2]), x);

@@ -40,9 +40,11 @@ def _arrays(g):
                              g["scalco"], g["samples"])
 
 
-def _search(method, g, params, **kw):
+def _search(method, g, params, variant=None, **kw):
     with semb.Plan(semb.params(method, **params, **kw)) as p:
         p.upload(_arrays(g).view())
+        if variant is not None:
+            p.set_variant(variant)
         p.run()
         return p.download()
 
@@ -116,3 +118,43 @@ def test_crs_block_with_2000_trace_apertures():
     _check_plain(_search(semb.CRS, g32, s.params, mode=semb.PLAIN_F32), ref32, rows, t0s)
     ref64 = oracle.crs(g64, s.params, "f64", cdps=rows, t0_range=(lo, hi), top2=True)
     _check_batched(_search(semb.CRS, g64, s.params, mode=semb.BATCHED), ref64, rows, t0s)
+
+
+SHARED_CENTRAL = 30   # CRS variant sharing the central traces' sums over A and B
+
+
+def _check_same_search(out, base):
+    """Two batched searches that differ only in the order of their FP32 sums: the same
+    picks but for near ties (which the re-pick may then settle the other way, moving
+    the semblance by the size of the tie) and semblances within a few FP32 roundings."""
+    assert np.mean(out[0] == base[0]) >= 0.999
+    np.testing.assert_allclose(out[1], base[1], atol=2e-5, rtol=1e-4)
+
+
+def test_crs_shared_central_traces_500x48_block():
+    """The CRS variant that leaves each task's central traces (zero midpoint distance)
+    out of the staged chunks and adds their sums, computed once per pass and C value,
+    to every (A, B) item: at the 500-CDP line's shapes it meets the batched bars against
+    the FP64 oracle and gives the default variant's results within float summation
+    order."""
+    s = synth.config(2)
+    g64 = oracle.gather(s.headers, s.samples, "crs", s.params["aph"], s.params["apm"], real=np.float64)
+    rows = np.arange(247, 253)
+    t0s = np.arange(0, 500)
+    ref64 = oracle.crs(g64, s.params, "f64", cdps=rows, t0_range=(0, 500), top2=True)
+    out = _search(semb.CRS, g64, s.params, variant=SHARED_CENTRAL, mode=semb.BATCHED)
+    _check_batched(out, ref64, rows, t0s)
+    base = _search(semb.CRS, g64, s.params, variant=13, mode=semb.BATCHED)
+    _check_same_search(out, base)
+
+
+def test_crs_shared_central_traces_2000_trace_block():
+    """The same variant on a block shaped like the 20k-CDP survey with ~2,000-trace
+    apertures (25 CDPs within apm, the central CDP's traces a 25th of each aperture):
+    the default variant's results within float summation order, on every CDP and t0."""
+    s = synth.crs_survey(seed=9, ncdp=64, ns=1500, dt_us=4000, nevents=6, tau=0.004, aph=2600, apm=150,
+                         azimuth=90.0, aperture_range=(1900, 2000), block=32, name="crs-block-ap2000")
+    g = oracle.gather(s.headers, s.samples, "crs", s.params["aph"], s.params["apm"], real=np.float64)
+    out = _search(semb.CRS, g, s.params, variant=SHARED_CENTRAL, mode=semb.BATCHED)
+    base = _search(semb.CRS, g, s.params, variant=13, mode=semb.BATCHED)
+    _check_same_search(out, base)
