@@ -44,8 +44,9 @@ struct ChunkTag {
   int t0s;
   int pass;
   int napert;
-  int ic_lo;   // Z0: the pass's first C index (its central sums are in the chunk's z0 slot)
-  int pad[2];
+  int ic_lo;   // Z0: the pass's first C index
+  int zslot;   // Z0: the pass slot of its central traces' sums
+  int pad;
 };
 
 // The planners' position in the chunk stream.
@@ -57,6 +58,9 @@ struct Producer {
   int next;   // index of the next chunk to produce
   float T_lo, T_hi;
   int64_t zb, ze;   // Z0: the task's central traces (entries zb .. ze-1)
+  int64_t zpos;     // Z0: the next central trace to add to the pass's sums
+  int pseq;         // Z0: passes started; the pass slot is pseq % kZ0Slots
+  int zslot, ic_lo; // Z0: the current pass's slot and first C index
 };
 
 // Shared-memory layout (bytes), shared by host and device:
@@ -69,8 +73,8 @@ struct Producer {
 //   kahan      Kahan totals and compensations [2][RC][NT]
 //   quad[3]    staged 16-byte entries, each followed by its zero block
 //   raw[2]     raw windows (TMA destination)
-//   z0[4]      Z0 variants: the central traces' sums carried by a pass's last chunk,
-//              [kZ0C][5][32] floats per chunk slot
+//   z0         Z0 variants: the central traces' sums of the passes in flight,
+//              [kZ0Slots][kZ0C][5][32] floats
 struct PipeLayout {
   size_t prod, meta, tag, src, z0, tops, kahan, quad, quad_stride, raw, raw_stride, total;
 };
@@ -84,7 +88,7 @@ __host__ __device__ inline PipeLayout pipe_layout(int rc, int cap, int storage, 
   L.tag = L.meta + kMetaRing * kMetaBytes;
   L.src = L.tag + align128(kMetaRing * sizeof(ChunkTag));
   L.z0 = L.src + (size_t)kMetaRing * kMaxChunk * 16;
-  L.tops = L.z0 + (z0 ? (size_t)kMetaRing * kZ0SlotFloats * 4 : 0);
+  L.tops = L.z0 + (z0 ? (size_t)kZ0Slots * kZ0SlotFloats * 4 : 0);
   L.kahan = L.tops + align128(3 * (size_t)kTopK * nt * 4);
   L.quad = L.kahan + align128(2 * (size_t)rc * nt * 4);
   // LAY_X3: a sample plane and a difference plane of kXPlane floats each (the plan
@@ -105,22 +109,24 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // t^2 = fma(t0, t0, C h) whatever A and B.  Computed with the items' own FP32
 // operations (the traveltime, its sample index and weight, and the interpolation of the
 // packed value/difference staging), so each trace adds what it would add to every
-// item of that C.  One lane per t0 of the task (lane = t0 - t0s), C indices c_lo ..
+// item of that C.  Adds central traces kb .. ke-1 (of the task's zb .. ze-1) to the
+// pass slot: one lane per t0 of the task (lane = t0 - t0s), C indices c_lo ..
 // c_lo + nc - 1; slot[(ci * 5 + q) * 32 + lane] holds the three window numerators, the
 // energy and the count of in-range traces (as a float).  Samples are read from the
 // trace store in global memory, within each trace's row (an in-range window ends at
 // most two samples past the record, inside the row's zero padding); a CDP's own traces
 // are consecutive in the store and in its aperture list.
-static __device__ __noinline__ void central_sums(const KParams& P, int t0s, int64_t zb, int64_t ze, int c_lo, int nc,
-                                                 float* slot) {
+static __device__ __noinline__ void central_add(const KParams& P, int t0s, int64_t zb, int64_t kb, int64_t ke,
+                                                int c_lo, int nc, float* slot) {
   const int lane = threadIdx.x & 31;
   const float T = (float)min(t0s + lane, P.ns - 1);
   const unsigned span = (unsigned)(P.ns - 2 * P.tau - 2);
-  const int tr0 = zb < ze ? __ldg(P.ap_tr + zb) : 0;
+  const int tr0 = kb < ke ? __ldg(P.ap_tr + zb) : 0;
   for (int ci = 0; ci < nc; ++ci) {
     const float cc = P.cvals[c_lo + ci];
-    float n0 = 0.f, n1 = 0.f, n2 = 0.f, den = 0.f, m = 0.f;
-    for (int64_t k = zb; k < ze; ++k) {
+    float* z = slot + ci * 5 * 32 + lane;
+    float n0 = z[0], n1 = z[32], n2 = z[64], den = z[96], m = z[128];
+    for (int64_t k = kb; k < ke; ++k) {
       const float4 g = __ldg(P.ap_geo + k);
       if (g.x != 0.f) continue;
       const float t = sqrt_fast(fmaf(T, T, cc * g.z));
@@ -155,7 +161,6 @@ static __device__ __noinline__ void central_sums(const KParams& P, int t0s, int6
       den = fmaf(w2, w2, den);
       m += 1.f;
     }
-    float* z = slot + ci * 5 * 32 + lane;
     z[0] = n0;
     z[32] = n1;
     z[64] = n2;
@@ -168,9 +173,10 @@ static __device__ __noinline__ void central_sums(const KParams& P, int t0s, int6
 // flight per iteration).
 // GLOB: as for semb_search_kernel, the variant may stage less than a whole trace.
 // Z0 (CRS B-run, packed value/difference staging): the planner leaves the task's
-// central traces at zero midpoint distance out of the chunks and, when it plans a
-// pass's last chunk, computes their sums for each C index of the pass into that
-// chunk's z0 slot (central_sums); each item adds those of its C when it finalizes.
+// central traces at zero midpoint distance out of the chunks and adds their sums for
+// each C index of the pass into the pass's slot, kZ0PerChunk traces with each chunk it
+// plans and the rest with the pass's last (central_add); each item adds those of its C
+// when it finalizes the pass.
 template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TU = 1, bool GLOB = false,
           bool Z0 = false>
 __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
@@ -179,7 +185,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const PipeLayout L = pipe_layout(RC, P.cap, P.storage, NT, LAY, Z0 ? 1 : 0);
   float* z0_base = reinterpret_cast<float*>(smem_raw + L.z0);
-  auto z0_at = [&](int c) { return z0_base + (size_t)(c % kMetaRing) * kZ0SlotFloats; };
+  auto z0_slot = [&](int slot) { return z0_base + (size_t)slot * kZ0SlotFloats; };
   constexpr uint32_t EB = lay_entry_bytes(LAY);   // bytes per staged entry
   uint64_t* raw_full = reinterpret_cast<uint64_t*>(smem_raw);   // [kRawBufs]
   uint64_t* q_full = raw_full + kRawBufs;                        // [kStages]
@@ -228,6 +234,9 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
     *merge_cnt = 0;
     prod->task = -1;
     prod->done = 0;
+    prod->pseq = 0;
+    prod->zslot = prod->ic_lo = 0;
+    prod->zpos = 0;
     prod->next = 0;
     fence_mbar_init();
   }
@@ -284,11 +293,29 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
     plan_chunk<METHOD, FORM_FAST>(P, P.pass_bounds + pass * 8, pos, end, prod->T_lo, prod->T_hi, m, src, prod->zb,
                                   prod->ze);
     const int64_t npos = pos + m->consumed;
-    if (Z0 && npos >= end) {
-      // the pass's last chunk carries the central traces' sums of the pass's C indices
+    if (Z0) {
+      // the central traces' sums of the pass: a new pass takes the next slot, zeroed;
+      // each chunk adds the next kZ0PerChunk traces, the pass's last chunk all the rest
       const int2 pc = P.pass_c[pass];
-      central_sums(P, prod->t0s, prod->zb, prod->ze, pc.x, pc.y, z0_at(c));
-      if (lane == 0) tg->ic_lo = pc.x;
+      const int slot = pos == begin ? prod->pseq % kZ0Slots : prod->zslot;
+      float* zs = z0_slot(slot);
+      int64_t kb = prod->zpos;
+      if (pos == begin) {
+        kb = prod->zb;
+        for (int q = lane; q < (int)kZ0SlotFloats; q += 32) zs[q] = 0.f;
+      }
+      const int64_t ke = npos >= end ? prod->ze : min(prod->ze, kb + kZ0PerChunk);
+      __syncwarp();
+      central_add(P, prod->t0s, prod->zb, kb, ke, pc.x, pc.y, zs);
+      __syncwarp();
+      if (lane == 0) {
+        if (pos == begin) prod->pseq += 1;
+        prod->zslot = slot;
+        prod->ic_lo = pc.x;
+        prod->zpos = ke;
+        tg->zslot = slot;
+        tg->ic_lo = pc.x;
+      }
     }
     if (lane == 0) {
       if (npos >= end) {
@@ -557,7 +584,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
         // the central traces' sums of this item's C index
         const int gi = __float_as_int(__ldg(&cand[r].w));
         if (gi >= 0) {
-          const float* z = z0_at(c) + (gi % P.nc_grid - tg.ic_lo) * 5 * 32 + lane;
+          const float* z = z0_slot(tg.zslot) + (gi % P.nc_grid - tg.ic_lo) * 5 * 32 + lane;
           fa[r].add_sums(z[0], z[32], z[64]);
           zden = z[96];
           fa[r].M += (int)z[128];
