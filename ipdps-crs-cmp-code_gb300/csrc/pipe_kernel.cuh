@@ -172,13 +172,13 @@ static __device__ __noinline__ void central_add(const KParams& P, int t0s, int64
 // TU: unroll factor of the in-range trace loop (independent work of TU traces in
 // flight per iteration).
 // GLOB: as for semb_search_kernel, the variant may stage less than a whole trace.
-// Z0 (CRS B-run, packed value/difference staging): the planner leaves the task's
+// Z0 > 0 (CRS B-run, packed value/difference staging): the planner leaves the task's
 // central traces at zero midpoint distance out of the chunks and adds their sums for
-// each C index of the pass into the pass's slot, kZ0PerChunk traces with each chunk it
-// plans and the rest with the pass's last (central_add); each item adds those of its C
-// when it finalizes the pass.
+// each C index of the pass into the pass's slot, Z0 traces with each chunk it plans and
+// the rest with the pass's last (central_add); each item adds those of its C when it
+// finalizes the pass.
 template <int METHOD, int W, int RC, int MINB, int LAY, bool BRUN, int NT, int TU = 1, bool GLOB = false,
-          bool Z0 = false>
+          int Z0 = 0>
 __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
   static_assert(!Z0 || (METHOD == METHOD_CRS && BRUN && W == 3 && stage_lay(LAY) == LAY_PD),
                 "central-trace sharing is for the CRS B-run packed value/difference kernel");
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
     const int64_t npos = pos + m->consumed;
     if (Z0) {
       // the central traces' sums of the pass: a new pass takes the next slot, zeroed;
-      // each chunk adds the next kZ0PerChunk traces, the pass's last chunk all the rest
+      // each chunk adds the next Z0 traces, the pass's last chunk all the rest
       const int2 pc = P.pass_c[pass];
       const int slot = pos == begin ? prod->pseq % kZ0Slots : prod->zslot;
       float* zs = z0_slot(slot);
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(NT, MINB) semb_pipe_kernel(KParams P) {
         kb = prod->zb;
         for (int q = lane; q < (int)kZ0SlotFloats; q += 32) zs[q] = 0.f;
       }
-      const int64_t ke = npos >= end ? prod->ze : min(prod->ze, kb + kZ0PerChunk);
+      const int64_t ke = npos >= end ? prod->ze : min(prod->ze, kb + (int64_t)Z0);
       __syncwarp();
       central_add(P, prod->t0s, prod->zb, kb, ke, pc.x, pc.y, zs);
       __syncwarp();

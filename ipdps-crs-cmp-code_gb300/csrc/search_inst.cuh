@@ -53,7 +53,7 @@ SearchEntry xp_entry() {
 }
 
 template <int METHOD, int W, int RC, int MINB, int LAY = LAY_P2, bool BRUN = false, int NT = 256, int TU = 1,
-          bool GLOB = false, bool Z0 = false>
+          bool GLOB = false, int Z0 = 0>
 SearchEntry pipe_entry() {
   return {(const void*)semb_pipe_kernel<METHOD, W, RC, MINB, LAY, BRUN, NT, TU, GLOB, Z0>, RC, MINB, BRUN ? 1 : 0, NT, 1,
           LAY, GLOB ? 1 : 0, Z0 ? 1 : 0};
@@ -134,9 +134,11 @@ SearchEntry search_entry(int w, int variant) {
       // variant 13 with 640 threads (20 warps per SM) at whole-trace stages
       if (variant == 28) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 640, 2>();
       if (variant == 29) return pipe_entry<METHOD, 3, (METHOD == METHOD_CMP ? 8 : 7), 1, LAY_PD, METHOD == METHOD_CRS, 640>();
-      // variant 13 with the central traces' sums shared over A and B
+      // variant 13 with the central traces' sums shared over A and B (8 or 4 of them
+      // added with each planned chunk)
       if constexpr (METHOD == METHOD_CRS) {
-        if (variant == 30) return pipe_entry<METHOD, 3, 7, 1, LAY_PD, true, 512, 2, false, true>();
+        if (variant == 30) return pipe_entry<METHOD, 3, 7, 1, LAY_PD, true, 512, 2, false, 8>();
+        if (variant == 31) return pipe_entry<METHOD, 3, 7, 1, LAY_PD, true, 512, 2, false, 4>();
       }
       break;
     case 5:

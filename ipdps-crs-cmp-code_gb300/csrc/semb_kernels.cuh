@@ -131,13 +131,11 @@ struct KParams {
   int nc_grid;
 };
 
-// Z0 variants: the most C indices one pass may span; the pass slots of the central
+// Z0 variants: the most C indices one pass may span, and the pass slots of the central
 // traces' sums (a slot is zeroed again at the start of the fourth pass after, when every
-// warp has finalized the pass that used it); the central traces each chunk's planner
-// adds to its pass's sums (the pass's last chunk adds all that are left)
+// warp has finalized the pass that used it)
 constexpr int kZ0C = 4;
 constexpr int kZ0Slots = 4;
-constexpr int kZ0PerChunk = 8;
 
 // ---------------------------------------------------------------------------
 // small PTX helpers (mbarrier + bulk copy)
