@@ -694,6 +694,21 @@ int copy_traces(semb_plan* pl, const semb_gather_view* g, int64_t t0, int64_t t1
   return SEMB_OK;
 }
 
+// Streamed upload: the traces of CDP chunks k0 .. k1-1 (pl->chunk_cdp) into the device
+// stores on stream cs, each chunk followed by its chunk_done event.
+int copy_chunks(semb_plan* pl, const semb_gather_view* g, int k0, int k1, cudaStream_t cs) {
+  for (int k = k0; k < k1; ++k) {
+    const int c0 = pl->chunk_cdp[k], c1 = pl->chunk_cdp[k + 1];
+    const int64_t t0 = c0 > 0 ? g->cdp_end[c0 - 1] : 0, t1 = c1 > 0 ? g->cdp_end[c1 - 1] : 0;
+    SEMB_TRY(copy_traces(pl, g, t0, t1, cs));
+    SEMB_CUDA(cudaEventRecord(pl->chunk_done[k], cs));
+  }
+  return SEMB_OK;
+}
+
+// streamed upload: chunks whose copies start before the set-up
+constexpr int kEarlyChunks = 2;
+
 int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   if (!pl || !g) return fail(SEMB_E_ARG, "null argument");
   const semb_params& p = pl->p;
@@ -760,31 +775,6 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   if (nchunks == 0) SEMB_TRY(copy_traces(pl, g, 0, ntr, cs));
   SEMB_CUDA(cudaEventRecord(pl->copy_done, cs));
   pl->nchunks = nchunks;
-  if (nchunks > 0) {
-    // streamed: CDP chunks of about equal trace counts in gather order.  Every chunk's
-    // copies are queued now, so that they run during the set-up below and during the
-    // search of the chunks before them; chunk_done[k] marks chunk k's traces in place.
-    pl->chunk_cdp.assign(1, 0);
-    for (int k = 1; k < nchunks; ++k) {
-      const int64_t target = g->ntraces * k / nchunks;
-      int c = pl->chunk_cdp.back();
-      while (c < g->ncdps && g->cdp_end[c] <= target) ++c;
-      pl->chunk_cdp.push_back(std::max(c, pl->chunk_cdp.back()));
-    }
-    pl->chunk_cdp.push_back(g->ncdps);
-    while ((int)pl->chunk_done.size() < nchunks) {
-      cudaEvent_t e;
-      SEMB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-      pl->chunk_done.push_back(e);
-    }
-    for (int k = 0; k < nchunks; ++k) {
-      const int c0 = pl->chunk_cdp[k], c1 = pl->chunk_cdp[k + 1];
-      const int64_t t0 = c0 > 0 ? g->cdp_end[c0 - 1] : 0, t1 = c1 > 0 ? g->cdp_end[c1 - 1] : 0;
-      SEMB_TRY(copy_traces(pl, g, t0, t1, cs));
-      SEMB_CUDA(cudaEventRecord(pl->chunk_done[k], cs));
-    }
-  }
-
   // header fields and CDP ranges (scratch for the set-up kernels)
   int32_t *d_gx, *d_gy, *d_sx, *d_sy, *d_sc;
   int64_t* d_cdp_end;
@@ -822,6 +812,27 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   SEMB_CUDA(cudaMemcpyAsync(d_sy, g->sy, ntr * 4, cudaMemcpyHostToDevice, st));
   SEMB_CUDA(cudaMemcpyAsync(d_sc, g->scalco, ntr * 4, cudaMemcpyHostToDevice, st));
   SEMB_CUDA(cudaMemcpyAsync(d_cdp_end, g->cdp_end, g->ncdps * 8, cudaMemcpyHostToDevice, st));
+  if (nchunks > 0) {
+    // streamed: CDP chunks of about equal trace counts in gather order.  The first
+    // chunks' copies are queued now, behind the header fields that the set-up needs
+    // first, so that they run during the set-up below; the others at the end of the
+    // set-up, after its own small copies, and during the search of the chunks before
+    // them.  chunk_done[k] marks chunk k's traces in place.
+    pl->chunk_cdp.assign(1, 0);
+    for (int k = 1; k < nchunks; ++k) {
+      const int64_t target = g->ntraces * k / nchunks;
+      int c = pl->chunk_cdp.back();
+      while (c < g->ncdps && g->cdp_end[c] <= target) ++c;
+      pl->chunk_cdp.push_back(std::max(c, pl->chunk_cdp.back()));
+    }
+    pl->chunk_cdp.push_back(g->ncdps);
+    while ((int)pl->chunk_done.size() < nchunks) {
+      cudaEvent_t e;
+      SEMB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      pl->chunk_done.push_back(e);
+    }
+    SEMB_TRY(copy_chunks(pl, g, 0, std::min(nchunks, kEarlyChunks), cs));
+  }
 
   const int tgrid = (int)std::min<int64_t>((ntr + 255) / 256, 65535);
   k_trace_geometry<<<tgrid, 256, 0, st>>>(ntr, d_gx, d_gy, d_sx, d_sy, d_sc, d_h32, d_mx32, d_my32, d_h64, d_mx64,
@@ -1041,6 +1052,8 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   if (set_all(pl, default_variant(p.method, form, pl->w)) != SEMB_OK &&
       set_all(pl, fallback_variant(p.method, form, pl->w)) != SEMB_OK)
     SEMB_TRY(set_all(pl, 0));
+  // streamed: the other chunks' copies, after the set-up's own small copies
+  if (nchunks > kEarlyChunks) SEMB_TRY(copy_chunks(pl, g, kEarlyChunks, nchunks, cs));
   SEMB_CUDA(cudaStreamWaitEvent(st, pl->copy_done, 0));   // the stores are complete for the run
   cudaEventRecord(pl->ev[5], st);
   SEMB_CUDA(cudaStreamSynchronize(st));
