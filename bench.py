@@ -103,6 +103,9 @@ def window_of(s) -> int:
     return 2 * max(tau, 0) + 1
 
 
+L2_BYTES = 129e6   # GB300 L2 cache
+
+
 def workload_config(name: str, s, method: int, world: int, mean_aperture: float | None) -> dict:
     """The `config` of both arms' JSON lines: the workload and its sizes."""
     ncand = int(s.params["nc"]) if method == semb.CMP else int(s.params["na"] * s.params["nb"] * s.params["nc"])
@@ -111,8 +114,9 @@ def workload_config(name: str, s, method: int, world: int, mean_aperture: float 
            "window": window_of(s), "traces": s.ntraces * world,
            "parallelism": (f"survey segments x{world} (one per rank, no collective)" if world > 1
                            else "single GPU"),
-           "l2": "inputs larger than L2 (FP32 %.2f GB, FP16 %.2f GB per GPU)" % (s.samples.nbytes / 1e9,
-                                                                                s.samples.nbytes / 2e9)}
+           "l2": ("inputs larger than L2 (FP32 %.2f GB, FP16 %.2f GB per GPU)" if s.samples.nbytes / 2 > L2_BYTES
+                  else "inputs within L2, no flush between steps (FP32 %.2f GB, FP16 %.2f GB per GPU)")
+                 % (s.samples.nbytes / 1e9, s.samples.nbytes / 2e9)}
     if mean_aperture is not None:
         cfg["mean_aperture"] = mean_aperture
         cfg["trace_evals_per_step"] = int(round(mean_aperture * ncdp * world)) * s.ns * ncand
