@@ -35,10 +35,10 @@
 extern "C" {
 #endif
 
-#define SEMB_ABI_VERSION 8
+#define SEMB_ABI_VERSION 9
 
 /* Search-kernel variant slots of semb_plan_autotune / semb_plan_set_variant. */
-#define SEMB_MAX_VARIANTS 32
+#define SEMB_MAX_VARIANTS 34
 
 /* Aperture buckets of a batched plan's work queue (semb_plan_buckets). */
 #define SEMB_MAX_BUCKETS 4

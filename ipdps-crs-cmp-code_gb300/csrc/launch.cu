@@ -32,24 +32,31 @@ int search_variant(int method, int form, int w, int v, int* rc, int* minb, int* 
   return e.fn != nullptr;
 }
 
+// Candidate slots of one (A, C) group's run of nb B values padded to a multiple of rc.
+static int brun_slots(int nb, int rc) { return (std::max(nb, 1) + rc - 1) / rc * rc; }
+
 // Variant a plan starts with (before any autotuning), the fastest measured on GB300
-// for the benchmark workloads of each window: for CRS the pipelined 512-thread B-run
-// kernel (packed value/difference staging with a two-way trace unroll and the central
-// traces' sums shared over A and B for w = 3, packed pairs otherwise); for CMP the
+// for the benchmark workloads of each window: for CRS the pipelined B-run kernel
+// (packed value/difference staging with a two-way trace unroll and the central traces'
+// sums shared over A and B for w = 3, packed pairs otherwise); for CMP the
 // two-barrier kernel with packed pairs (w = 3) or packed pairs formed by scalar FMAs
-// (w = 5); variant 0 elsewhere.  fallback_variant() is the one to use where the default
-// does not fit the plan (a grid whose passes span more C values than variant 30 takes).
-int default_variant(int method, int form, int w) {
+// (w = 5); variant 0 elsewhere.  For CRS with w = 3 the B-run length follows the
+// grid's nb: runs of 7 (variant 30, 512 threads) unless nb pads less to a multiple of
+// 8 (variant 33, 384 threads; nb = 31 takes 32 slots per (A, C) instead of 35; per
+// slot the two run at the same speed).  fallback_variant() is the one to use where the
+// default does not fit the plan (a grid whose passes span more C values than the
+// central-trace sharing takes).
+int default_variant(int method, int form, int w, int nb) {
   if (form != FORM_FAST) return 0;
-  if (method == METHOD_CRS && w == 3) return 30;
+  if (method == METHOD_CRS && w == 3) return brun_slots(nb, 8) < brun_slots(nb, 7) ? 33 : 30;
   if (method == METHOD_CRS && w <= 5) return 14;
   if (method == METHOD_CMP && w == 3) return 8;
   if (method == METHOD_CMP && w == 5) return 21;
   return 0;
 }
 
-int fallback_variant(int method, int form, int w) {
-  if (form == FORM_FAST && method == METHOD_CRS && w == 3) return 13;
+int fallback_variant(int method, int form, int w, int nb) {
+  if (form == FORM_FAST && method == METHOD_CRS && w == 3) return brun_slots(nb, 8) < brun_slots(nb, 7) ? 32 : 13;
   return 0;
 }
 

@@ -38,8 +38,8 @@ constexpr int kBucketSplits = 3;
 constexpr int kBucketAp[kBucketSplits] = {1024, 384, 128};
 static_assert(kBucketSplits + 1 <= kMaxBuckets, "bucket table");
 int search_occupancy(int method, int form, int w, int variant, int nwarps, size_t smem, int* ctas_per_sm);
-int default_variant(int method, int form, int w);
-int fallback_variant(int method, int form, int w);
+int default_variant(int method, int form, int w, int nb);
+int fallback_variant(int method, int form, int w, int nb);
 int grid_neighbours(int ncdps, const float* d_fmx, const float* d_fmy, int apm, int64_t* d_off, int32_t** d_list,
                     int64_t* n_out, cudaStream_t st);
 // CDP count from which the CRS neighbour lists come from the grid search
@@ -1049,8 +1049,8 @@ int upload_impl(semb_plan* pl, const semb_gather_view* g, int nchunks) {
   for (int i = 0; i < g->ncdps; ++i) pl->aperture[i] = (int32_t)(ap_off[i + 1] - ap_off[i]);
 
   // the default variant of this method and window; variant 0 where it does not fit
-  if (set_all(pl, default_variant(p.method, form, pl->w)) != SEMB_OK &&
-      set_all(pl, fallback_variant(p.method, form, pl->w)) != SEMB_OK)
+  if (set_all(pl, default_variant(p.method, form, pl->w, p.nb)) != SEMB_OK &&
+      set_all(pl, fallback_variant(p.method, form, pl->w, p.nb)) != SEMB_OK)
     SEMB_TRY(set_all(pl, 0));
   // streamed: the other chunks' copies, after the set-up's own small copies
   if (nchunks > kEarlyChunks) SEMB_TRY(copy_chunks(pl, g, kEarlyChunks, nchunks, cs));

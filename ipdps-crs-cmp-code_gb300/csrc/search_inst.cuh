@@ -139,6 +139,12 @@ SearchEntry search_entry(int w, int variant) {
       if constexpr (METHOD == METHOD_CRS) {
         if (variant == 30) return pipe_entry<METHOD, 3, 7, 1, LAY_PD, true, 512, 2, false, 8>();
         if (variant == 31) return pipe_entry<METHOD, 3, 7, 1, LAY_PD, true, 512, 2, false, 4>();
+        // B runs of 8 for grids whose nb pads less to a multiple of 8 than of 7 (nb = 31:
+        // 32 slots per (A, C) instead of 35): variant 13 with RC = 8 (128 registers, no
+        // spills), and the central-trace sharing at 384 threads, where RC = 8 fits in
+        // 156 registers (at 512 threads it would spill)
+        if (variant == 32) return pipe_entry<METHOD, 3, 8, 1, LAY_PD, true, 512, 2>();
+        if (variant == 33) return pipe_entry<METHOD, 3, 8, 1, LAY_PD, true, 384, 2, false, 8>();
       }
       break;
     case 5:

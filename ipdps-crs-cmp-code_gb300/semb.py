@@ -31,8 +31,8 @@ PLAIN_F32, BATCHED = 0, 1
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 REPICK_OFF, REPICK_NEAR_TIES, REPICK_ALWAYS = 0, 1, 2
 DM_ABS, DM_SIGNED = 0, 1
-ABI_VERSION = 8
-MAX_VARIANTS = 32   # SEMB_MAX_VARIANTS
+ABI_VERSION = 9
+MAX_VARIANTS = 34   # SEMB_MAX_VARIANTS
 MAX_BUCKETS = 4     # SEMB_MAX_BUCKETS
 
 OK, E_ARG, E_IO, E_FORMAT, E_WINDOW, E_NOMEM, E_CUDA, E_TIMEOUT, E_STATE, E_NODEV, E_BOUNDS = range(11)

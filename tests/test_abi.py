@@ -27,7 +27,7 @@ def test_library_exports_every_declared_symbol(semb_lib):
 
 def test_versions_and_messages(semb_lib):
     lib = semb.lib()
-    assert lib.semb_abi_version() == semb.ABI_VERSION == 8
+    assert lib.semb_abi_version() == semb.ABI_VERSION == 9
     assert lib.semb_strerror(semb.OK) == b"ok"
     assert lib.semb_strerror(semb.E_NODEV) == b"no usable CUDA device"
     assert lib.semb_strerror(12345) == b"unknown error"

@@ -158,3 +158,23 @@ def test_crs_shared_central_traces_2000_trace_block():
     out = _search(semb.CRS, g, s.params, variant=SHARED_CENTRAL, mode=semb.BATCHED)
     base = _search(semb.CRS, g, s.params, variant=13, mode=semb.BATCHED)
     _check_same_search(out, base)
+
+
+def test_crs_b_runs_of_8_on_a_31_value_b_axis():
+    """nb = 31, the B axis of the 100,000-CDP survey's 31^3 grid: B runs of 8 pad each
+    (A, C) group to 32 candidate slots where runs of 7 pad it to 35, so the plan starts
+    on variant 33 (runs of 8, central traces' sums shared, 384 threads).  It and variant
+    32 (runs of 8, 512 threads) meet the batched bars against the FP64 oracle and give
+    variant 13's results (runs of 7) within float summation order."""
+    s = synth.crs_survey(seed=41, ncdp=24, noffsets=16, ns=400, dt_us=4000, na=3, nb=31, nc=3, tau=0.004, apm=50)
+    g64 = oracle.gather(s.headers, s.samples, "crs", s.params["aph"], s.params["apm"], real=np.float64)
+    rows, t0s = np.arange(9, 15), np.arange(0, 400)
+    ref64 = oracle.crs(g64, s.params, "f64", cdps=rows, t0_range=(0, 400), top2=True)
+    with semb.Plan(semb.params(semb.CRS, mode=semb.BATCHED, **s.params)) as p:
+        p.upload(_arrays(g64).view())
+        assert [b[3] for b in p.buckets()] == [33] * len(p.buckets())
+    base = _search(semb.CRS, g64, s.params, variant=13, mode=semb.BATCHED)
+    for v in (33, 32):
+        out = _search(semb.CRS, g64, s.params, variant=v, mode=semb.BATCHED)
+        _check_batched(out, ref64, rows, t0s)
+        _check_same_search(out, base)
