@@ -541,7 +541,10 @@ def run_chunked_survey(args):
         t_up = time.perf_counter()
         plan.upload(gather_arrays(s, cdp_end).view())
         out["upload_s"] = time.perf_counter() - t_up
-        if args.tune:
+        if args.variant is not None:
+            plan.set_variant(args.variant)
+            out["variant"] = args.variant
+        elif args.tune:
             t_tune = time.perf_counter()
             v, ms = plan.autotune()
             out["autotune"] = {"variant": v, "sample_ms": ms, "seconds": time.perf_counter() - t_tune,
